@@ -1,0 +1,294 @@
+/*
+ * lattice.h -- C ABI of the GB300 lattice engine.
+ *
+ * The engine evolves interacting scalar fields on a periodic 3D lattice with
+ * the symplectic kick-drift (leapfrog / Yoshida) scheme of the Fortran lattice
+ * codes, on one sm_103a GPU.  Every entry point below replaces one Fortran
+ * module procedure of the reference; the replaced routine is cited beside it
+ * (paths are relative to the reference project root).  A Fortran driver binds
+ * these through iso_c_binding; Python binds them through ctypes.
+ *
+ * Conventions (all entry points):
+ *  - return an int status (LAT_OK == 0); nothing aborts the process;
+ *    lat_last_error() gives a one-line message for the calling thread;
+ *  - a handle owns its device memory and one CUDA stream; handles are not
+ *    thread-safe, distinct handles may be used from distinct threads;
+ *  - the caller owns every host array; host field arrays use the Fortran
+ *    layout fld(nfld, i, j, k) with the field index fastest and optional
+ *    ghost padding (lo/hi sites per side), as in the reference drivers;
+ *  - fields stay resident in HBM between calls; copies happen only in
+ *    upload / download / output calls.
+ */
+#ifndef LATTICE_GB300_H
+#define LATTICE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum lat_status {
+  LAT_OK = 0,
+  LAT_ERR_ARG = 1,         /* bad argument / configuration                 */
+  LAT_ERR_CUDA = 2,        /* CUDA runtime or cuFFT error                  */
+  LAT_ERR_TIMEOUT = 3,     /* a bounded device wait gave up                */
+  LAT_ERR_NAN = 4,         /* NaN/Inf in an FP64 reduction                 */
+  LAT_ERR_ALLOC = 5,       /* device or host allocation failed             */
+  LAT_ERR_STATE = 6,       /* call not valid in the handle's state         */
+  LAT_ERR_IO = 7,          /* checkpoint file error                        */
+  LAT_ERR_UNSUPPORTED = 8  /* valid request this build does not implement  */
+};
+
+/* ---------------------------------------------------------- configuration */
+enum lat_laplacian {
+  LAT_LAP_SPECTRAL = 1,  /* FFT Laplacian, Pseudospec/openmp_dev/fftw_mod.f90:177-207 */
+  LAT_LAP_FD7 = 7,       /* 7-point stencil, Discrete/Bubble-Collisions/params.f90:116 */
+  LAT_LAP_FD27 = 27      /* 27-point stencil, Discrete/Bubble-Collisions/params.f90:119, macros.h:31-44 */
+};
+
+enum lat_background {
+  LAT_BG_MINKOWSKI = 0,  /* Pseudospec/openmp_dev/hamiltonian_minkowski.f90 */
+  LAT_BG_CONFORMAL = 1   /* Pseudospec/openmp_dev/hamiltonian_conformal.f90 (self-consistent a) */
+};
+
+enum lat_precision {
+  LAT_FP64 = 0,          /* plain FP64 fields (the reference's -r8)        */
+  LAT_FP32_KAHAN = 1     /* FP32 fields, Kahan-compensated drift, FP64 reductions */
+};
+
+/* Order of the Hamiltonian pieces inside symp_o2step.
+ *  PSEUDOSPEC: 1 = fields kinetic (drift), 2 = gravity kinetic (conformal
+ *    only), last = gradient+potential (kick);
+ *    Pseudospec/openmp_dev/hamiltonian_conformal.f90:50-81.
+ *  DEFROST: 1 = metric kinetic, 2 = fields kinetic, 3 = gradient+potential;
+ *    Discrete/Bubble-Collisions/evolve.f90:98-113,225-240. */
+enum lat_split_order { LAT_SPLIT_PSEUDOSPEC = 0, LAT_SPLIT_DEFROST = 1 };
+
+enum lat_model {
+  LAT_MODEL_PHI4 = 0,        /* V = lam/4 phi^4 (params[0]=lam); hamiltonian_minkowski.f90:161-186 */
+  LAT_MODEL_PHI4_G2 = 1,     /* V = lam/4 phi^4 + g2/2 phi^2 chi^2 (params: lam, g2), nfld = 2;
+                                Pseudospec/mpi_dev/hamiltonian_conformal_rksplit.f90:220-237 */
+  LAT_MODEL_DOUBLE_WELL = 2, /* V = (phi^2-1)^2/4 - del (phi+1) (params[0]=del);
+                                Discrete/Bubble-Collisions/model.f90:96-165 */
+  LAT_MODEL_FREE = 3         /* V = sum_f m2/2 phi_f^2 (params[0]=m2), known-answer model */
+};
+
+typedef struct lat_config {
+  int32_t nx, ny, nz;        /* lattice sites per side (x fastest)          */
+  int32_t nfld;              /* number of real scalar fields                */
+  double len;                /* box side along x; dx = len/nx, dk = 2 pi/(n dx) */
+  int32_t laplacian;         /* enum lat_laplacian                          */
+  int32_t background;        /* enum lat_background                         */
+  int32_t precision;         /* enum lat_precision                          */
+  int32_t split_order;       /* enum lat_split_order                        */
+  int32_t model;             /* enum lat_model                              */
+  int32_t gw;                /* 1: evolve the six u_ij and pi_ij (FD, Minkowski) */
+  double model_params[4];
+  double stencil[5];         /* (c0,c1,c2,c3,cc); all zero = default of the chosen stencil */
+  double gw_coupling;        /* kappa in pi_ij' = lap u_ij + kappa d_i phi d_j phi */
+  int32_t device;            /* CUDA ordinal                                */
+  int32_t reserved[7];
+} lat_config;
+
+typedef struct lat_s lat_t;
+
+/* ---------------------------------------------------------------- errors */
+const char* lat_last_error(void);
+const char* lat_version(void);
+
+/* ---------------------------------------------------------------- handle */
+/* Allocates fields, FFT plans and scratch.  Replaces the module-global
+ * arrays and plans of Pseudospec/openmp_dev/hamiltonian_conformal.f90:22-38
+ * and initialize_arrays, evolve_spectral.f90:107-127. */
+int lat_create(lat_t** out, const lat_config* cfg);
+int lat_destroy(lat_t* h);
+int lat_get_config(const lat_t* h, lat_config* cfg);
+
+/* Host <-> device copies of the state in the Fortran layout
+ * fld(nfld, 1-lo : n+hi, ...) (ghost sites are ignored on upload and left
+ * untouched on download).  Pseudospec: fld lo=hi=1, fldp lo=hi=0
+ * (hamiltonian_conformal.f90:22-23); DEFROST: lo=2, hi=3
+ * (Discrete/Bubble-Collisions/latpar.f90:78-80). */
+int lat_upload(lat_t* h, const double* fld, int32_t fld_lo, int32_t fld_hi,
+               const double* fldp, int32_t fldp_lo, int32_t fldp_hi);
+int lat_download(lat_t* h, double* fld, int32_t fld_lo, int32_t fld_hi,
+                 double* fldp, int32_t fldp_lo, int32_t fldp_hi);
+
+/* Scale factor yscl and its conjugate momentum ysclp (conformal only).
+ * get_scale_factor / get_hubble, hamiltonian_conformal.f90:242-250. */
+int lat_set_scale_factor(lat_t* h, double a, double ap);
+int lat_get_scale_factor(lat_t* h, double* a, double* ap);
+/* Friedmann constraint: ysclp = -sqrt(12 a^4 rho). calc_metric,
+ * hamiltonian_conformal.f90:263-304. */
+int lat_calc_metric(lat_t* h);
+
+/* ------------------------------------------------------------ integrator */
+/* symp2/4/6/8 (order 2,4,6,8), Pseudospec/openmp_dev/evolve_spectral.f90:129-227
+ * and Discrete/Bubble-Collisions/evolve.f90:118-223.  The whole call runs
+ * asynchronously on the handle's stream without host synchronisation. */
+int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps);
+/* symp_o2step(dt,w1,w2), hamiltonian_conformal.f90:50-64. */
+int lat_o2step(lat_t* h, double dt, double w1, double w2);
+/* Hamiltonian_Split(dt, hamind), hamiltonian_conformal.f90:66-81 and
+ * Discrete/Bubble-Collisions/evolve.f90:225-240. */
+int lat_split(lat_t* h, double dt, int32_t hamind);
+/* Substep clocks tglobal(1:3), Discrete/Bubble-Collisions/evolve.f90:39. */
+int lat_get_time(lat_t* h, double tglobal[3]);
+/* Blocks until the handle's stream is idle; reports device-side errors. */
+int lat_sync(lat_t* h);
+
+/* -------------------------------------------------------------- Laplacian */
+/* Laplacian of field `field` (0-based) with the configured operator, written
+ * to out(nx,ny,nz).  laplacian_3d, Pseudospec/openmp_dev/fftw_mod.f90:177-207;
+ * FD: STENCIL(c,LAPLACE)/(cc dx^2), Discrete/Bubble-Collisions/evolve.f90:271-281. */
+int lat_laplacian(lat_t* h, int32_t field, double* out);
+/* Stand-alone laplacian_3d(n1,n2,n3,f,Fk,dk,planf,planb): f(n1,n2,n3) is
+ * replaced by its spectral Laplacian, FP64 (fftw_mod.f90:177-207). */
+int lat_laplacian_3d(int32_t n1, int32_t n2, int32_t n3, double* f, double dk);
+
+/* ------------------------------------------------------------- energies */
+enum lat_energy_index {
+  LAT_E_KE = 0,        /* 1/2 <pi^2> / a^6                       */
+  LAT_E_GE_LAP = 1,    /* -1/2 <phi lap phi> / a^2               */
+  LAT_E_GE_GRAD = 2,   /* 1/2 <(grad phi)^2> / a^2 (stencil form) */
+  LAT_E_PE = 3,        /* <V>                                     */
+  LAT_E_RHO = 4,       /* KE + GE_LAP + PE                        */
+  LAT_E_GRAV = 5,      /* -3 H^2, H = -ysclp/(6 a^2)              */
+  LAT_E_RESIDUAL = 6,  /* (rho + grav)/rho                        */
+  LAT_E_A = 7,
+  LAT_E_AP = 8,
+  LAT_E_MEAN0 = 9,     /* <phi_1>                                 */
+  LAT_E_MEAN1 = 10,    /* <phi_2> (0 for one field)               */
+  LAT_E_GW = 11,       /* 1/2 <pi_ij pi_ij> + 1/2 <grad u_ij . grad u_ij> (gw only) */
+  LAT_NENERGY = 12
+};
+/* dump_rho, Pseudospec/openmp_dev/evolve_spectral.f90:305-415; homlat
+ * grad_en / grad_en_wlap / pot_en / kinetic_en,
+ * Discrete/Bubble-Collisions/homlat.f90:65-188. */
+int lat_energies(lat_t* h, double out[LAT_NENERGY]);
+
+/* --------------------------------------------------------------- spectra */
+enum lat_spec_what { LAT_SPEC_FLD = 0, LAT_SPEC_FLDP = 1 };
+enum lat_spec_mode {
+  LAT_SPEC_WEIGHTED = 0,  /* two-bin smooth weights, spectrum_3d, Pseudospec/openmp_dev/analysis_spec.f90:59-102 */
+  LAT_SPEC_COUNT = 1      /* floor(|n|)+1 with integer counts, spectrum_bin, Discrete/Bubble-Collisions/analysis.f90:193-223 */
+};
+/* Number of bins of spectrum_3d: floor(sqrt((nx/2+1)^2+(ny/2+1)^2+(nz/2+1)^2+1)),
+ * init_spectrum_3d, analysis_spec.f90:48-57. */
+int lat_spectrum_nbins(const lat_t* h, int32_t* ns);
+/* S(l) = sum_k c |F_k|^2 / W(l) with the unnormalised forward DFT F_k of
+ * the chosen array; W is the weight sum (WEIGHTED) or the integer mode count
+ * (COUNT, stored exactly in the doubles).  Bins beyond ns come back zero. */
+int lat_spectrum(lat_t* h, int32_t what, int32_t field, int32_t mode,
+                 int32_t nbins, double* S, double* W);
+/* crossspec_3d(Fk1,Fk2,S_real,S_imag), analysis_spec.f90:145-178. */
+int lat_crossspec(lat_t* h, int32_t what1, int32_t field1, int32_t what2,
+                  int32_t field2, int32_t nbins, double* S_re, double* S_im);
+/* Stand-alone spectrum_3d(S,f,Fk,plan) of a host array f(n1,n2,n3). */
+int lat_spectrum_3d(int32_t n1, int32_t n2, int32_t n3, const double* f,
+                    int32_t mode, int32_t nbins, double* S, double* W);
+
+/* ---------------------------------------------------- gravitational waves */
+/* TT-projected GW spectrum: sum over modes of sum_ij |Lambda_ij,lm pi_lm(k)|^2
+ * per integer shell (spectrum_bin binning), divided by the count W.
+ * Storage hij/pi_hij, grav-waves/data-gw.f90:14-40; drift h += pi dt,
+ * grav-waves/evolve-gw.f90:38-44; the projector is the empty stub of
+ * grav-waves/gw-projectors.f90:13-26. */
+int lat_gw_spectrum(lat_t* h, int32_t nbins, double* S, double* W);
+/* u_ij / pi_ij host copies, component order 11,22,33,12,13,23, each (nx,ny,nz). */
+int lat_gw_download(lat_t* h, double* u, double* pu);
+int lat_gw_upload(lat_t* h, const double* u, const double* pu);
+
+/* ---------------------------------------------------- initial conditions */
+/* Vacuum fluctuations drawn mode by mode in k space with a counter-based
+ * generator keyed by (seed, field, mode) so that CPU and GPU draw identical
+ * fields: <|F_k|^2> = amp N^2 / (2 V w_k), w_k = sqrt(k^2 + m2eff[f]),
+ * pi_k = -i w_k F_k (a wave travelling along +k; the Hermitian partner of a
+ * drawn mode inside the kx = 0 and kx = nx/2 planes carries +i w_k F_k and a
+ * self-conjugate mode none), |k| > kcut_frac * pi/dx and k = 0 zeroed; then
+ * fld = fld0[f] + IDFT(F)/N, fldp = dfld0[f] + IDFT(pi_k)/N.  Replaces
+ * init_fields/sample, Pseudospec/openmp_dev/evolve_spectral.f90:262-303,421-506
+ * (whose draw depends on the compiler's random_number). */
+int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0,
+                    const double* dfld0, const double* m2eff, double amp,
+                    double kcut_frac);
+/* Thin-wall bubbles phi = -1 + sum_b [1 - tanh((r_b - R)/width)], zero momentum;
+ * centres in lattice units of length (x,y,z per bubble).  Replaces
+ * init_fields/initbubble, Discrete/Bubble-Collisions/ic_bubble.f90:17-123. */
+int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres,
+                     double radius, double width);
+
+/* -------------------------------------------------------------- checkpoint */
+/* Raw native-double checkpoint fld_<i>.raw / fldp_<i>.raw (interior only,
+ * x fastest) plus checkpt.dat "yscl ysclp / time / outframenum";
+ * make_check_pt / read_check_pt, Discrete/Bubble-Collisions/scafld.f90:227-287
+ * and driver.f90:71-91,117-129.  `dir` must exist. */
+int lat_checkpoint_write(lat_t* h, const char* dir, double time, int32_t frame);
+int lat_checkpoint_read(lat_t* h, const char* dir, double* time, int32_t* frame);
+
+/* ------------------------------------------------------------- ensembles */
+/* A batch of independent runs of one model on lattices of uneven size,
+ * advanced together: per-size batched FFT plans and one persistent launch
+ * per pass over a (run, tile) work list, the whole step captured in a CUDA
+ * graph.  Spectral Laplacian, Minkowski, FP32-Kahan or FP64.  No reference
+ * counterpart (the reference runs one lattice per job). */
+typedef struct lat_ens_s lat_ens_t;
+int lat_ens_create(lat_ens_t** out, const lat_config* base, int32_t nruns,
+                   const int32_t* sizes /* n per run, cubic */);
+int lat_ens_destroy(lat_ens_t* e);
+int lat_ens_init_vacuum(lat_ens_t* e, const uint64_t* seeds, double fld0,
+                        double dfld0, double m2eff, double amp, double kcut_frac);
+int lat_ens_symp(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps);
+int lat_ens_energies(lat_ens_t* e, double* out /* nruns x LAT_NENERGY */);
+int lat_ens_spectrum(lat_ens_t* e, int32_t run, int32_t nbins, double* S, double* W);
+int lat_ens_download(lat_ens_t* e, int32_t run, double* fld, double* fldp);
+int lat_ens_sync(lat_ens_t* e);
+
+/* ---------------------------------------------------------- measurement */
+/* Kernel classes timed with CUDA events on the handle's stream when
+ * timing is enabled (one event pair per launch). */
+enum lat_kclass {
+  LAT_K_KICKDRIFT = 0,   /* fused kick+drift pass (FD stencil or spectral pointwise) */
+  LAT_K_DRIFT = 1,
+  LAT_K_KICK = 2,
+  LAT_K_KMUL = 3,        /* k-space -k^2/N multiply (+ Parseval reduction) */
+  LAT_K_FFT_R2C = 4,     /* cuFFT forward */
+  LAT_K_FFT_C2R = 5,     /* cuFFT inverse */
+  LAT_K_GW = 6,          /* GW kick+drift */
+  LAT_K_OTHER = 7,
+  LAT_NKCLASS = 8
+};
+int lat_timing_enable(lat_t* h, int32_t on);
+/* total milliseconds and launch count of one class since the last reset */
+int lat_timing_read(lat_t* h, int32_t kclass, double* total_ms, int64_t* launches);
+int lat_timing_reset(lat_t* h);
+/* Records CUDA event `slot` (0..15) on the handle's stream; lat_mark_elapsed
+ * waits for both events and returns the device time between them. */
+int lat_mark(lat_t* h, int32_t slot);
+int lat_mark_elapsed(lat_t* h, int32_t slot_a, int32_t slot_b, double* ms);
+/* number of engine kernels launched on this handle since creation */
+int lat_launch_count(const lat_t* h, int64_t* count);
+/* Device pointers of the state, for zero-copy harnesses.  what: 0 = fld,
+ * 1 = fldp, 2 = Kahan compensation of fld (FP32 only), 3 = scalar block.
+ * Element type is double (FP64) or float (FP32_KAHAN), layout [field][z][y][x]. */
+int lat_device_ptr(lat_t* h, int32_t what, void** ptr);
+/* Pinned host memory for staging (cudaHostAlloc / cudaFreeHost). */
+int lat_host_alloc(void** ptr, size_t bytes);
+int lat_host_free(void* ptr);
+
+/* -------------------------------------------------------------- autotune */
+/* Times the candidate tile shapes / block schedules of this handle's kernels
+ * on its own lattice (state is saved and restored) and keeps the fastest;
+ * results are cached in `cache_path` (JSON lines) keyed by size, precision,
+ * stencil and device, and reused when present.  cache_path may be NULL. */
+int lat_autotune(lat_t* h, const char* cache_path);
+/* The tile choice in use: tx, ty, zchunk, block threads, blocks per SM. */
+int lat_tuning_get(const lat_t* h, int32_t out[5]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LATTICE_GB300_H */

@@ -1,0 +1,157 @@
+// engine.hpp -- host-side structures of the GB300 lattice engine and the
+// launchers each kernel translation unit exports.
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace lat {
+
+// Set the thread's error message and return `code`.
+int set_error(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+// ------------------------------------------------------------ FD passes
+// One tiled stencil pass: kick (and optionally drift) of the fields and,
+// with gw, of the six u_ij.  Tiles of 32 x ty sites march along z in chunks
+// of zc planes; the 3x3 in-plane neighbourhood of each plane is staged in
+// shared memory and the three-plane window is kept in registers.
+struct FdArgs {
+  int nx, ny, nz, nf;
+  const void* phi_in;  // fields read by the stencil
+  void* phi_out;       // drifted fields (fused pass), nullptr for kick only
+  void* phic;          // Kahan compensation (FP32 only), updated in place
+  void* pi;            // momenta, updated in place
+  const void* u_in;    // GW strain read by the stencil (nullptr: no GW)
+  void* u_out;         // drifted strain (fused pass)
+  void* pu;            // GW momenta
+  double lc[4];        // stencil coefficients c_r / (cc dx^2)
+  int seven;           // 7-point stencil (c2 = c3 = 0)
+  ModelP model;
+  double hk, hd;       // kick and drift sizes
+  double kappa, inv2dx;
+  int conf;            // conformal kick: a from the scalar block, GE2/PE reductions, ysclp update
+  double Nd;
+  DevScalars* sc;
+  RedBuf rb;
+  int ty, zc;          // tile: 32 x ty threads, zc planes per block
+};
+int launch_fd(const FdArgs& a, int precision, cudaStream_t s, int* nblocks_out);
+int fd_max_blocks(int nx, int ny, int nz, int ty, int zc);
+
+// ------------------------------------------------------ pointwise passes
+enum PwMode { PW_KD = 0, PW_DRIFT = 1, PW_KICK = 2 };
+struct PwArgs {
+  int64_t N;
+  int nf;
+  void* phi;          // fields, updated in place by drifts
+  void* phic;         // Kahan compensation (FP32)
+  void* pi;
+  const void* lap;    // Laplacian (spectral, already divided by N) for kicks
+  void* u;            // GW strain (drift only), nullptr if none
+  const void* pu;
+  ModelP model;
+  double hk, hg, hd;  // kick, gravity half-kick and drift sizes
+  double Nd;
+  int conf;
+  int mode;           // PwMode
+  DevScalars* sc;
+  RedBuf rb;
+  int grid, block;
+};
+int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s);
+
+// k-space multiply F *= -k^2/N with the Parseval sum of k^2|F|^2 (Hermitian
+// weights) into sc->ge2 when store_ge2 is set.
+struct KmulArgs {
+  int nx, ny, nz, nf;
+  void* Fk;
+  double dkx2, dky2, dkz2, invN;
+  int store_ge2;
+  DevScalars* sc;
+  RedBuf rb;
+  int grid, block;
+};
+int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s);
+// a -= h * ap / 6 on the device (Hamiltonian_grav_kinetic)
+int launch_grav(DevScalars* sc, double h, cudaStream_t s);
+
+// ------------------------------------------------------- output kernels
+int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c,
+                   cudaStream_t s);
+int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos,
+                   cudaStream_t s);
+int launch_to_fp64(const void* hi, const void* c, int64_t n, int precision, double* out, cudaStream_t s);
+int launch_from_fp64(const double* in, int64_t n, int precision, void* hi, void* c, cudaStream_t s);
+
+struct SpecArgs {
+  int nx, ny, nz;
+  const void* F1;  // half spectrum [z][y][nx/2+1]
+  const void* F2;  // second spectrum for the cross spectrum (nullptr otherwise)
+  int mode;        // LAT_SPEC_WEIGHTED / LAT_SPEC_COUNT / 2 = cross (weighted)
+  int nbins;
+  double* partials;   // [grid][3*nbins]
+  double* out;        // [3*nbins]: S (or S_re), W, S_im
+  unsigned int* counter;
+  int grid, block;
+};
+int launch_spectrum(const SpecArgs& a, int precision, cudaStream_t s);
+
+struct GwSpecArgs {
+  int nx, ny, nz;
+  const void* F[6];
+  double dx;
+  int nbins;
+  double* partials;
+  double* out;  // [2*nbins]
+  unsigned int* counter;
+  int grid, block;
+};
+int launch_gw_spectrum(const GwSpecArgs& a, int precision, cudaStream_t s);
+
+// Energies: raw lattice sums into sc->red:
+// [0] sum pi^2, [1] sum V, [2] sum phi_1, [3] sum phi_2, [4] -sum phi L phi (FD),
+// [5] sum STENCIL(c,GRAD2) (FD), [6] sum pu^2, [7] -sum u L u (GW, weighted)
+struct EnergyArgs {
+  int nx, ny, nz, nf;
+  const void* phi;
+  const void* phic;
+  const void* pi;
+  const void* u;
+  const void* pu;
+  int fd;  // FD sums [4],[5],[7]
+  double c[4];  // raw stencil coefficients c0..c3
+  ModelP model;
+  DevScalars* sc;
+  RedBuf rb;
+  int grid, block;
+};
+int launch_energy(const EnergyArgs& a, int precision, cudaStream_t s);
+// sum over the half spectrum of w k^2 |F|^2 (Parseval) into sc->red[slot]
+int launch_parseval(const void* Fk, int nx, int ny, int nz, int nf, double dkx2, double dky2,
+                    double dkz2, DevScalars* sc, int slot, RedBuf rb, int grid, int precision,
+                    cudaStream_t s);
+
+struct VacArgs {
+  int nx, ny, nz;
+  uint64_t seed;
+  int field;
+  double dkx, dky, dkz, sig_pref;  // sig = sqrt(sig_pref / w)
+  double m2, kcut;
+  double2* Fphi;
+  double2* Fpi;
+};
+int launch_vacuum_modes(const VacArgs& a, cudaStream_t s);
+int launch_fd_laplacian64(const double* in, double* out, int nx, int ny, int nz, const double* lc, cudaStream_t s);
+int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStream_t s);
+int launch_bubbles(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* centres_dev,
+                   double radius, double width, cudaStream_t s);
+
+// bookkeeping of launches for the kernel-launch census
+extern thread_local int64_t* g_launch_counter;
+
+}  // namespace lat

@@ -1,0 +1,485 @@
+// k_out.cu -- layout conversion, spectra, energies and initial conditions.
+#include "engine.hpp"
+
+namespace lat {
+
+namespace {
+
+// ------------------------------------------------------------ layouts
+// Fortran fld(nfld, i, j, k) (field fastest) <-> device [field][z][y][x].
+template <typename R, bool KAHAN>
+__global__ void aos2soa_kernel(const double* __restrict__ aos, int nf, int64_t N, R* hi, R* c) {
+  const int64_t tot = N * nf;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t / nf;
+    const int f = (int)(t - s * nf);
+    const double v = aos[t];
+    const R h = (R)v;
+    hi[f * N + s] = h;
+    if (KAHAN && c) c[f * N + s] = (R)((double)h - v);
+  }
+}
+template <typename R, bool KAHAN>
+__global__ void soa2aos_kernel(const R* hi, const R* c, int nf, int64_t N, double* __restrict__ aos) {
+  const int64_t tot = N * nf;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t / nf;
+    const int f = (int)(t - s * nf);
+    double v = (double)hi[f * N + s];
+    if (KAHAN && c) v -= (double)c[f * N + s];
+    aos[t] = v;
+  }
+}
+template <typename R, bool KAHAN>
+__global__ void to64_kernel(const R* hi, const R* c, int64_t n, double* out) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    double v = (double)hi[t];
+    if (KAHAN && c) v -= (double)c[t];
+    out[t] = v;
+  }
+}
+template <typename R, bool KAHAN>
+__global__ void from64_kernel(const double* in, int64_t n, R* hi, R* c) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = in[t];
+    const R h = (R)v;
+    hi[t] = h;
+    if (KAHAN && c) c[t] = (R)((double)h - v);
+  }
+}
+
+inline int grid_for(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+inline int done(const char* what) {
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, what);
+}
+
+// ------------------------------------------------------------ spectra
+// Array grid reduction: every block adds its shared bins to partials[block],
+// the last block sums the rows in block order.
+__device__ void bins_grid_reduce(const double* shb, int nval, double* partials, double* out,
+                                 unsigned int* counter) {
+  __shared__ int am_last;
+  const int bid = blockIdx.x;
+  for (int i = threadIdx.x; i < nval; i += blockDim.x) partials[(size_t)bid * nval + i] = shb[i];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  for (int i = threadIdx.x; i < nval; i += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(&partials[(size_t)b * nval + i]);
+    out[i] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// Binning of spectrum_3d (analysis_spec.f90:86-99) / spectrum_bin
+// (Discrete/Bubble-Collisions/analysis.f90:203-214).  The reference loops over
+// the full x range with folded ii, i.e. Hermitian weight 2 on interior kx
+// planes.  Shell index l = floor(sqrt(ii^2+jj^2+kk^2)) is taken exactly in
+// integers; the smooth weights use the correctly rounded FP64 sqrt and
+// uncontracted FP64 arithmetic so they are bit-identical to the host's.
+template <typename R, typename C>
+__global__ void __launch_bounds__(256) spec_kernel(SpecArgs a) {
+  extern __shared__ double shb[];  // [3][nbins]
+  const int nb = a.nbins;
+  for (int i = threadIdx.x; i < 3 * nb; i += blockDim.x) shb[i] = 0.0;
+  __syncthreads();
+  const C* F1 = static_cast<const C*>(a.F1);
+  const C* F2 = static_cast<const C*>(a.F2);
+  const unsigned int hx = a.nx / 2 + 1, ny = a.ny;
+  const unsigned int M = hx * ny * (unsigned int)a.nz;
+  for (unsigned int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const int x = (int)(m % hx);
+    const unsigned int r = m / hx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const int jj = fold_idx(y, a.ny), kk = fold_idx(z, a.nz);
+    const double wx = (x == 0 || 2 * x == a.nx) ? 1.0 : 2.0;
+    const int m2 = x * x + jj * jj + kk * kk;
+    const int l = isqrt_exact(m2);
+    const C f1 = F1[m];
+    double v, vi = 0.0;
+    if (a.mode == 2) {
+      const C f2 = F2[m];
+      v = (double)f1.x * (double)f2.x + (double)f1.y * (double)f2.y;   // Re(F1 conj F2)
+      vi = (double)f1.y * (double)f2.x - (double)f1.x * (double)f2.y;  // Im(F1 conj F2)
+    } else {
+      v = (double)f1.x * (double)f1.x + (double)f1.y * (double)f1.y;
+    }
+    if (a.mode == LAT_SPEC_COUNT) {
+      if (l < nb) {
+        atomicAdd(&shb[l], wx * v);
+        atomicAdd(&shb[nb + l], wx);
+      }
+    } else {
+      const double p = sqrt((double)m2);
+      const double d0 = __dsub_rn((double)l, p), d1 = __dsub_rn((double)(l + 1), p);
+      const double e0 = __dsub_rn(1.0, __dmul_rn(d0, d0)), e1 = __dsub_rn(1.0, __dmul_rn(d1, d1));
+      const double c0 = __dmul_rn(e0, e0), c1 = __dmul_rn(e1, e1);
+      if (l < nb) {
+        atomicAdd(&shb[l], wx * c0 * v);
+        atomicAdd(&shb[nb + l], wx * c0);
+        if (a.mode == 2) atomicAdd(&shb[2 * nb + l], wx * c0 * vi);
+      }
+      if (l + 1 < nb) {
+        atomicAdd(&shb[l + 1], wx * c1 * v);
+        atomicAdd(&shb[nb + l + 1], wx * c1);
+        if (a.mode == 2) atomicAdd(&shb[2 * nb + l + 1], wx * c1 * vi);
+      }
+    }
+  }
+  __syncthreads();
+  bins_grid_reduce(shb, 3 * nb, a.partials, a.out, a.counter);
+}
+
+// TT projection of the six pi_ij with the lattice momentum of the central
+// difference, k_i = sin(2 pi n_i / N_i)/dx:  P = 1 - k k^T/k^2,
+// pi^TT = P pi P - P tr(P pi)/2;  sum_ij |pi^TT_ij|^2 binned like spectrum_bin.
+template <typename R, typename C>
+__global__ void __launch_bounds__(256) gwspec_kernel(GwSpecArgs a) {
+  extern __shared__ double shb[];  // [2][nbins]
+  const int nb = a.nbins;
+  for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x) shb[i] = 0.0;
+  __syncthreads();
+  const unsigned int hx = a.nx / 2 + 1, ny = a.ny;
+  const unsigned int M = hx * ny * (unsigned int)a.nz;
+  const double twopi = 6.283185307179586476925286766559;
+  for (unsigned int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const int x = (int)(m % hx);
+    const unsigned int r = m / hx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const int jj = fold_idx(y, a.ny), kk = fold_idx(z, a.nz);
+    const double wx = (x == 0 || 2 * x == a.nx) ? 1.0 : 2.0;
+    const int l = isqrt_exact(x * x + jj * jj + kk * kk);
+    if (l >= nb) continue;
+    double k[3] = {sin(twopi * x / a.nx) / a.dx, sin(twopi * y / a.ny) / a.dx, sin(twopi * z / a.nz) / a.dx};
+    const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    double sum = 0.0;
+    if (k2 > 0.0) {
+      double P[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) P[i][j] = (i == j ? 1.0 : 0.0) - k[i] * k[j] / k2;
+      const int map[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+      double hr[3][3], hi[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const C v = static_cast<const C*>(a.F[map[i][j]])[m];
+          hr[i][j] = (double)v.x;
+          hi[i][j] = (double)v.y;
+        }
+      double Ar[3][3], Ai[3][3];  // A = P h
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double sr = 0, si = 0;
+#pragma unroll
+          for (int l2 = 0; l2 < 3; ++l2) { sr += P[i][l2] * hr[l2][j]; si += P[i][l2] * hi[l2][j]; }
+          Ar[i][j] = sr; Ai[i][j] = si;
+        }
+      double trr = Ar[0][0] + Ar[1][1] + Ar[2][2], tri = Ai[0][0] + Ai[1][1] + Ai[2][2];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double sr = 0, si = 0;
+#pragma unroll
+          for (int l2 = 0; l2 < 3; ++l2) { sr += Ar[i][l2] * P[l2][j]; si += Ai[i][l2] * P[l2][j]; }
+          sr -= 0.5 * P[i][j] * trr;
+          si -= 0.5 * P[i][j] * tri;
+          sum += sr * sr + si * si;
+        }
+    }
+    atomicAdd(&shb[l], wx * sum);
+    atomicAdd(&shb[nb + l], wx);
+  }
+  __syncthreads();
+  bins_grid_reduce(shb, 2 * nb, a.partials, a.out, a.counter);
+}
+
+// ------------------------------------------------------------ energies
+template <typename R, bool KAHAN, int NF>
+__global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int64_t N = (int64_t)nx * ny * nz;
+  const R* phi = static_cast<const R*>(a.phi);
+  const R* pi = static_cast<const R*>(a.pi);
+  const R* u = static_cast<const R*>(a.u);
+  const R* pu = static_cast<const R*>(a.pu);
+  using Acc = typename AccOf<R>::type;
+  Acc s[8];
+  const R c0 = (R)a.c[0], c1 = (R)a.c[1], c2 = (R)a.c[2], c3 = (R)a.c[3];
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    R f[NF];
+#pragma unroll
+    for (int l = 0; l < NF; ++l) {
+      f[l] = phi[l * N + t];
+      const R p = pi[l * N + t];
+      s[0].add(p * p);
+    }
+    s[1].add(model_v<R, NF>(a.model, f));
+    s[2].add(f[0]);
+    if (NF > 1) s[3].add(f[NF > 1 ? 1 : 0]);
+    if (a.fd || u) {
+      const int x = (int)(t % nx), y = (int)((t / nx) % ny), z = (int)(t / ((int64_t)nx * ny));
+      auto wrapi = [](int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); };
+      auto stencil = [&](const R* g, R& lapsum, R& grad2) {
+        const R g0 = g[t];
+        R r1 = 0, r2 = 0, r3 = 0, q1 = 0, q2 = 0, q3 = 0;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int rank = (dx != 0) + (dy != 0) + (dz != 0);
+              if (rank == 0) continue;
+              const R v = g[((int64_t)wrapi(z + dz, nz) * ny + wrapi(y + dy, ny)) * nx + wrapi(x + dx, nx)];
+              const R d = v - g0;
+              if (rank == 1) { r1 += v; q1 += d * d; }
+              else if (rank == 2) { r2 += v; q2 += d * d; }
+              else { r3 += v; q3 += d * d; }
+            }
+        lapsum = c0 * g0 + c1 * r1 + c2 * r2 + c3 * r3;
+        grad2 = c1 * q1 + c2 * q2 + c3 * q3;
+      };
+      if (a.fd) {
+#pragma unroll
+        for (int l = 0; l < NF; ++l) {
+          R ls, g2;
+          stencil(phi + l * N, ls, g2);
+          s[4].add(-f[l] * ls);
+          s[5].add(g2);
+        }
+      }
+      if (u) {
+        for (int g = 0; g < 6; ++g) {
+          const R w = g < 3 ? R(1) : R(2);
+          const R p = pu[g * N + t];
+          s[6].add(w * p * p);
+          R ls, g2;
+          stencil(u + g * N, ls, g2);
+          s[7].add(-w * u[g * N + t] * ls);
+        }
+      }
+    }
+  }
+  double v[8], tot[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = s[i].val();
+  if (grid_reduce<8>(v, a.rb, tot)) {
+    for (int i = 0; i < 8; ++i) {
+      a.sc->red[i] = tot[i];
+      if (bad(tot[i])) a.sc->err |= 1u;
+    }
+  }
+}
+
+template <typename R, typename C>
+__global__ void __launch_bounds__(256) parseval_kernel(const C* F, int nx, int ny, int nz, int nf, double dkx2,
+                                                       double dky2, double dkz2, DevScalars* sc, int slot,
+                                                       RedBuf rb) {
+  const unsigned int hx = nx / 2 + 1;
+  const unsigned int M = hx * (unsigned int)ny * (unsigned int)nz;
+  double acc = 0.0;
+  for (unsigned int m = blockIdx.x * blockDim.x + threadIdx.x; m < M * (unsigned int)nf; m += gridDim.x * blockDim.x) {
+    const unsigned int mm = m % M;
+    const int x = (int)(mm % hx);
+    const unsigned int r = mm / hx;
+    const int y = (int)(r % (unsigned int)ny), z = (int)(r / (unsigned int)ny);
+    const int jj = fold_idx(y, ny), kk = fold_idx(z, nz);
+    const double k2 = (double)(x * x) * dkx2 + (double)(jj * jj) * dky2 + (double)(kk * kk) * dkz2;
+    const double w = (x == 0 || 2 * x == nx) ? 1.0 : 2.0;
+    const C v = F[m];
+    acc += w * k2 * ((double)v.x * v.x + (double)v.y * v.y);
+  }
+  double vv[1] = {acc}, t[1];
+  if (grid_reduce<1>(vv, rb, t)) sc->red[slot] = t[0];
+}
+
+// -------------------------------------------------- initial conditions
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double u01(uint64_t r) { return ((double)(r >> 11) + 1.0) * (1.0 / 9007199254740992.0); }
+__device__ __forceinline__ double2 mode_gauss(uint64_t seed, int field, int64_t mode) {
+  const uint64_t key = mix64(mix64(mix64(seed) ^ (uint64_t)field) ^ (uint64_t)mode);
+  const double u1 = u01(mix64(key ^ 1ULL)), u2 = u01(mix64(key ^ 2ULL));
+  const double r = sqrt(-2.0 * log(u1));
+  const double th = 6.2831853071795864769252867665590 * u2;
+  return make_double2(r * cos(th), r * sin(th));
+}
+
+// Same draw as the oracle's orc_init_vacuum: Hermitian partners inside the
+// kx = 0 and kx = nx/2 planes share one draw (the lower mode index draws).
+__global__ void vacuum_kernel(VacArgs a) {
+  const int hx = a.nx / 2 + 1;
+  const int64_t M = (int64_t)hx * a.ny * a.nz;
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(m % hx);
+    const int64_t r = m / hx;
+    const int y = (int)(r % a.ny), z = (int)(r / a.ny);
+    const int jj = fold_idx(y, a.ny), kk = fold_idx(z, a.nz);
+    const double k2 = (double)x * x * a.dkx * a.dkx + (double)jj * jj * a.dky * a.dky + (double)kk * kk * a.dkz * a.dkz;
+    double2 F = make_double2(0, 0), P = make_double2(0, 0);
+    if (k2 > 0.0 && sqrt(k2) <= a.kcut) {
+      const double w = sqrt(k2 + a.m2);
+      const double sig = sqrt(a.sig_pref / w);
+      const bool selfplane = (x == 0) || (2 * x == a.nx);
+      const int64_t mp = ((int64_t)((a.nz - z) % a.nz) * a.ny + (a.ny - y) % a.ny) * hx + x;
+      const double h = 0.70710678118654752440084436210485;
+      // pi_k = -i w F_k for the drawing member of a pair (a wave travelling along
+      // +k); the Hermitian partner carries +i w F, a self-conjugate mode none.
+      if (selfplane && mp == m) {
+        double2 g = mode_gauss(a.seed, a.field, m);
+        F = make_double2(sig * g.x, 0.0);
+      } else if (selfplane && mp < m) {
+        double2 g = mode_gauss(a.seed, a.field, mp);
+        F = make_double2(sig * g.x * h, -(sig * g.y * h));
+        P = make_double2(-w * F.y, w * F.x);  // +i w F
+      } else {
+        double2 g = mode_gauss(a.seed, a.field, m);
+        F = make_double2(sig * g.x * h, sig * g.y * h);
+        P = make_double2(w * F.y, -w * F.x);  // -i w F
+      }
+    }
+    a.Fphi[m] = F;
+    a.Fpi[m] = P;
+  }
+}
+
+// STENCIL(c,LAPLACE) with pre-scaled coefficients lc = c/(cc dx^2), FP64.
+__global__ void fd_lap64_kernel(const double* g, double* out, int nx, int ny, int nz, double l0, double l1, double l2,
+                                double l3) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % nx), y = (int)((t / nx) % ny), z = (int)(t / ((int64_t)nx * ny));
+    double r1 = 0, r2 = 0, r3 = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int rank = (dx != 0) + (dy != 0) + (dz != 0);
+          if (rank == 0) continue;
+          const int xx = x + dx < 0 ? x + dx + nx : (x + dx >= nx ? x + dx - nx : x + dx);
+          const int yy = y + dy < 0 ? y + dy + ny : (y + dy >= ny ? y + dy - ny : y + dy);
+          const int zz = z + dz < 0 ? z + dz + nz : (z + dz >= nz ? z + dz - nz : z + dz);
+          const double v = g[((int64_t)zz * ny + yy) * nx + xx];
+          if (rank == 1) r1 += v; else if (rank == 2) r2 += v; else r3 += v;
+        }
+    out[t] = l0 * g[t] + l1 * r1 + l2 * r2 + l3 * r3;
+  }
+}
+
+__global__ void add_scale_kernel(double* f, int64_t n, double scale, double offset) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    f[t] = offset + f[t] * scale;
+}
+
+__global__ void bubbles_kernel(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* cen,
+                               double R, double w) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % nx), y = (int)((t / nx) % ny), z = (int)(t / ((int64_t)nx * ny));
+    double v = -1.0;
+    for (int b = 0; b < nbub; ++b) {
+      const double rx = x * dx - cen[3 * b], ry = y * dx - cen[3 * b + 1], rz = z * dx - cen[3 * b + 2];
+      const double rr = sqrt(rx * rx + ry * ry + rz * rz);
+      v += 1.0 - tanh((rr - R) / w);
+    }
+    phi[t] = v;
+  }
+}
+
+}  // namespace
+
+int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c, cudaStream_t s) {
+  if (precision == LAT_FP64) aos2soa_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, (double*)hi, nullptr);
+  else aos2soa_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, (float*)hi, (float*)c);
+  return done("aos2soa");
+}
+int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos, cudaStream_t s) {
+  if (precision == LAT_FP64) soa2aos_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>((const double*)hi, nullptr, nf, N, aos);
+  else soa2aos_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>((const float*)hi, (const float*)c, nf, N, aos);
+  return done("soa2aos");
+}
+int launch_to_fp64(const void* hi, const void* c, int64_t n, int precision, double* out, cudaStream_t s) {
+  if (precision == LAT_FP64) to64_kernel<double, false><<<grid_for(n), 256, 0, s>>>((const double*)hi, nullptr, n, out);
+  else to64_kernel<float, true><<<grid_for(n), 256, 0, s>>>((const float*)hi, (const float*)c, n, out);
+  return done("to_fp64");
+}
+int launch_from_fp64(const double* in, int64_t n, int precision, void* hi, void* c, cudaStream_t s) {
+  if (precision == LAT_FP64) from64_kernel<double, false><<<grid_for(n), 256, 0, s>>>(in, n, (double*)hi, nullptr);
+  else from64_kernel<float, true><<<grid_for(n), 256, 0, s>>>(in, n, (float*)hi, (float*)c);
+  return done("from_fp64");
+}
+
+int launch_spectrum(const SpecArgs& a, int precision, cudaStream_t s) {
+  const size_t smem = (size_t)3 * a.nbins * sizeof(double);
+  if (precision == LAT_FP64) spec_kernel<double, double2><<<a.grid, a.block, smem, s>>>(a);
+  else spec_kernel<float, float2><<<a.grid, a.block, smem, s>>>(a);
+  return done("spectrum");
+}
+
+int launch_gw_spectrum(const GwSpecArgs& a, int precision, cudaStream_t s) {
+  const size_t smem = (size_t)2 * a.nbins * sizeof(double);
+  if (precision == LAT_FP64) gwspec_kernel<double, double2><<<a.grid, a.block, smem, s>>>(a);
+  else gwspec_kernel<float, float2><<<a.grid, a.block, smem, s>>>(a);
+  return done("gw spectrum");
+}
+
+int launch_energy(const EnergyArgs& a, int precision, cudaStream_t s) {
+  if (a.nf == 1) {
+    if (precision == LAT_FP64) energy_kernel<double, false, 1><<<a.grid, a.block, 0, s>>>(a);
+    else energy_kernel<float, true, 1><<<a.grid, a.block, 0, s>>>(a);
+  } else if (a.nf == 2) {
+    if (precision == LAT_FP64) energy_kernel<double, false, 2><<<a.grid, a.block, 0, s>>>(a);
+    else energy_kernel<float, true, 2><<<a.grid, a.block, 0, s>>>(a);
+  } else {
+    return set_error(LAT_ERR_UNSUPPORTED, "energies support nfld = 1 or 2");
+  }
+  return done("energy");
+}
+
+int launch_parseval(const void* Fk, int nx, int ny, int nz, int nf, double dkx2, double dky2, double dkz2,
+                    DevScalars* sc, int slot, RedBuf rb, int grid, int precision, cudaStream_t s) {
+  if (precision == LAT_FP64)
+    parseval_kernel<double, double2><<<grid, 256, 0, s>>>((const double2*)Fk, nx, ny, nz, nf, dkx2, dky2, dkz2, sc, slot, rb);
+  else
+    parseval_kernel<float, float2><<<grid, 256, 0, s>>>((const float2*)Fk, nx, ny, nz, nf, dkx2, dky2, dkz2, sc, slot, rb);
+  return done("parseval");
+}
+
+int launch_vacuum_modes(const VacArgs& a, cudaStream_t s) {
+  const int64_t M = (int64_t)(a.nx / 2 + 1) * a.ny * a.nz;
+  vacuum_kernel<<<grid_for(M), 256, 0, s>>>(a);
+  return done("vacuum");
+}
+int launch_fd_laplacian64(const double* in, double* out, int nx, int ny, int nz, const double* lc, cudaStream_t s) {
+  fd_lap64_kernel<<<grid_for((int64_t)nx * ny * nz), 256, 0, s>>>(in, out, nx, ny, nz, lc[0], lc[1], lc[2], lc[3]);
+  return done("fd laplacian");
+}
+int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStream_t s) {
+  add_scale_kernel<<<grid_for(n), 256, 0, s>>>(f, n, scale, offset);
+  return done("add_scale");
+}
+int launch_bubbles(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* cen, double R, double w,
+                   cudaStream_t s) {
+  bubbles_kernel<<<grid_for((int64_t)nx * ny * nz), 256, 0, s>>>(phi, nx, ny, nz, dx, nbub, cen, R, w);
+  return done("bubbles");
+}
+
+}  // namespace lat

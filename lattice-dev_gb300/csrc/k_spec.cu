@@ -1,0 +1,287 @@
+// k_spec.cu -- pointwise kick / drift passes and the k-space multiply.
+//
+// Restates, for the spectral Laplacian,
+//   Hamiltonian_fields_kin      Pseudospec/openmp_dev/hamiltonian_conformal.f90:92-118
+//   Hamiltonian_grav_kinetic    hamiltonian_conformal.f90:86-90
+//   Hamiltonian_fields_grad_pot hamiltonian_conformal.f90:128-174,203-205
+//   laplacian_3d k-space loop   Pseudospec/openmp_dev/fftw_mod.f90:192-201
+// (Minkowski: hamiltonian_minkowski.f90:86-136).
+//
+// Fusion.  symp_o2step applies  G(h/2) K(h) G(h/2) D(h')  per substep.  The
+// kick's Friedmann update needs GE2 = -sum phi lap / a^2 and PE = sum V(phi),
+// both functions of phi alone: GE2 comes from the k-space pass by Parseval
+// (sum_x phi lap = -(1/N) sum_k k^2 |F_k|^2) and PE from the previous drift
+// pass.  Every block of the fused pass therefore knows a, ysclp before and
+// after the kick and the drift coefficient h'/a^2 before it starts, and kick
+// and drift run as ONE sweep over HBM.  The drift's KE2 and the new PE are
+// reduced deterministically and the last block applies the ysclp update.
+#include "engine.hpp"
+
+namespace lat {
+
+namespace {
+
+template <typename R> struct Vec4;
+template <> struct Vec4<float> {
+  float v[4];
+  __device__ __forceinline__ void load(const float* p) {
+    float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+  __device__ __forceinline__ void store(float* p) const {
+    __stcs(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+  }
+};
+template <> struct Vec4<double> {
+  double v[4];
+  __device__ __forceinline__ void load(const double* p) {
+    double2 a = __ldcs(reinterpret_cast<const double2*>(p));
+    double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+  __device__ __forceinline__ void store(double* p) const {
+    __stcs(reinterpret_cast<double2*>(p), make_double2(v[0], v[1]));
+    __stcs(reinterpret_cast<double2*>(p) + 1, make_double2(v[2], v[3]));
+  }
+};
+
+struct Coef {
+  double a0, ap0, a1, ap1, a2;
+  double ck, cv, cd;
+};
+
+// Scalar chain of one pass, identical in every block.
+__device__ __forceinline__ Coef coefs(const PwArgs& a, bool conf) {
+  Coef c{};
+  if (!conf) {
+    c.ck = a.hk; c.cv = a.hk; c.cd = a.hd;
+    return c;
+  }
+  const DevScalars* sc = a.sc;
+  c.a0 = __ldcg(&sc->a);
+  c.ap0 = __ldcg(&sc->ap);
+  if (a.mode == PW_KD) {
+    c.a1 = c.a0 - a.hg * c.ap0 / 6.0;                        // G(h/2)
+    const double GE2 = __ldcg(&sc->ge2) / (c.a1 * c.a1) / a.Nd;
+    const double PE = __ldcg(&sc->pe);
+    c.ap1 = c.ap0 - c.a1 * c.a1 * c.a1 * (GE2 + 4.0 * PE) * a.hk;  // K(h) scalar part
+    c.a2 = c.a1 - a.hg * c.ap1 / 6.0;                        // G(h/2)
+    c.ck = a.hk * c.a1 * c.a1;
+    c.cv = a.hk * c.a1 * c.a1 * c.a1 * c.a1;
+    c.cd = a.hd / (c.a2 * c.a2);
+  } else if (a.mode == PW_DRIFT) {
+    c.cd = a.hd / (c.a0 * c.a0);
+  } else {
+    c.ck = a.hk * c.a0 * c.a0;
+    c.cv = a.hk * c.a0 * c.a0 * c.a0 * c.a0;
+  }
+  return c;
+}
+
+template <typename R, bool KAHAN, int NF, bool CONF, int MODE, bool GWD>
+__global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
+  const Coef co = coefs(a, CONF);
+  const R ck = (R)co.ck, cv = (R)co.cv, cd = (R)co.cd;
+  const int64_t N = a.N;
+  R* phi = static_cast<R*>(a.phi);
+  R* phic = static_cast<R*>(a.phic);
+  R* pi = static_cast<R*>(a.pi);
+  const R* lap = static_cast<const R*>(a.lap);
+  using Acc = typename AccOf<R>::type;
+  Acc acc_ke, acc_pe, acc_ge;
+
+  auto site = [&](R (&f)[NF], R (&c)[NF], R (&p)[NF], const R (&lp)[NF]) {
+    if (MODE == PW_KD || MODE == PW_KICK) {
+      R dv[NF];
+      model_dv<R, NF>(a.model, f, dv);
+#pragma unroll
+      for (int l = 0; l < NF; ++l) {
+        if (CONF && MODE == PW_KICK) acc_ge.add(-f[l] * lp[l]);
+        p[l] = p[l] + (ck * lp[l] - cv * dv[l]);
+      }
+      if (CONF && MODE == PW_KICK) acc_pe.add(model_v<R, NF>(a.model, f));
+    }
+    if (MODE == PW_KD || MODE == PW_DRIFT) {
+#pragma unroll
+      for (int l = 0; l < NF; ++l) {
+        if constexpr (KAHAN) kahan_add(f[l], c[l], cd * p[l]);
+        else f[l] = f[l] + cd * p[l];
+        if (CONF) acc_ke.add(p[l] * p[l]);
+      }
+      if (CONF) acc_pe.add(model_v<R, NF>(a.model, f));
+    }
+  };
+
+  const int64_t nvec = N / 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += stride) {
+    const int64_t s0 = v * 4;
+    Vec4<R> F[NF], C[NF], P[NF], L[NF];
+#pragma unroll
+    for (int l = 0; l < NF; ++l) {
+      F[l].load(phi + l * N + s0);
+      if (KAHAN && MODE != PW_KICK) C[l].load(phic + l * N + s0);
+      P[l].load(pi + l * N + s0);
+      if (MODE != PW_DRIFT) L[l].load(lap + l * N + s0);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      R f[NF], c[NF], p[NF], lp[NF];
+#pragma unroll
+      for (int l = 0; l < NF; ++l) {
+        f[l] = F[l].v[j];
+        c[l] = (KAHAN && MODE != PW_KICK) ? C[l].v[j] : R(0);
+        p[l] = P[l].v[j];
+        lp[l] = MODE != PW_DRIFT ? L[l].v[j] : R(0);
+      }
+      site(f, c, p, lp);
+#pragma unroll
+      for (int l = 0; l < NF; ++l) {
+        F[l].v[j] = f[l];
+        C[l].v[j] = c[l];
+        P[l].v[j] = p[l];
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NF; ++l) {
+      if (MODE != PW_KICK) F[l].store(phi + l * N + s0);
+      if (KAHAN && MODE != PW_KICK) C[l].store(phic + l * N + s0);
+      if (MODE != PW_DRIFT) P[l].store(pi + l * N + s0);
+    }
+  }
+  // tail (N not a multiple of 4)
+  for (int64_t s = nvec * 4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
+    R f[NF], c[NF], p[NF], lp[NF];
+#pragma unroll
+    for (int l = 0; l < NF; ++l) {
+      f[l] = phi[l * N + s];
+      c[l] = (KAHAN && MODE != PW_KICK) ? phic[l * N + s] : R(0);
+      p[l] = pi[l * N + s];
+      lp[l] = MODE != PW_DRIFT ? lap[l * N + s] : R(0);
+    }
+    site(f, c, p, lp);
+#pragma unroll
+    for (int l = 0; l < NF; ++l) {
+      if (MODE != PW_KICK) phi[l * N + s] = f[l];
+      if (KAHAN && MODE != PW_KICK) phic[l * N + s] = c[l];
+      if (MODE != PW_DRIFT) pi[l * N + s] = p[l];
+    }
+  }
+  if (GWD) {  // u_ij += h' pu_ij (Minkowski drift of the strain, grav-waves/evolve-gw.f90:38-44)
+    R* u = static_cast<R*>(a.u);
+    const R* pu = static_cast<const R*>(a.pu);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < 6 * N; s += stride)
+      u[s] = u[s] + cd * pu[s];
+  }
+
+  if (CONF) {
+    double v[3] = {acc_ke.val(), acc_pe.val(), acc_ge.val()}, tot[3];
+    if (grid_reduce<3>(v, a.rb, tot)) {
+      DevScalars* sc = a.sc;
+      if (bad(tot[0]) || bad(tot[1]) || bad(tot[2])) sc->err |= 1u;
+      if (MODE == PW_KD) {
+        sc->a = co.a2;
+        sc->ap = co.ap1 + a.hd * (tot[0] / a.Nd) / (co.a2 * co.a2 * co.a2);
+        sc->pe = tot[1] / a.Nd;
+        sc->ke2 = tot[0];
+      } else if (MODE == PW_DRIFT) {
+        sc->ap = co.ap0 + a.hd * (tot[0] / a.Nd) / (co.a0 * co.a0 * co.a0);
+        sc->pe = tot[1] / a.Nd;
+        sc->ke2 = tot[0];
+      } else {
+        const double GE2 = tot[2] / (co.a0 * co.a0) / a.Nd;
+        const double PE = tot[1] / a.Nd;
+        sc->ap = co.ap0 - co.a0 * co.a0 * co.a0 * (GE2 + 4.0 * PE) * a.hk;
+        sc->pe = PE;
+      }
+    }
+  }
+}
+
+template <typename R, bool KAHAN, int NF, bool CONF>
+int pw_go(const PwArgs& a, cudaStream_t s) {
+  const bool gw = a.u != nullptr;
+  switch (a.mode) {
+    case PW_KD: pw_kernel<R, KAHAN, NF, CONF, PW_KD, false><<<a.grid, a.block, 0, s>>>(a); break;
+    case PW_DRIFT:
+      if (gw) pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, true><<<a.grid, a.block, 0, s>>>(a);
+      else pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, false><<<a.grid, a.block, 0, s>>>(a);
+      break;
+    case PW_KICK: pw_kernel<R, KAHAN, NF, CONF, PW_KICK, false><<<a.grid, a.block, 0, s>>>(a); break;
+    default: return set_error(LAT_ERR_ARG, "bad pointwise mode");
+  }
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "pointwise launch");
+}
+
+template <typename R, bool KAHAN, int NF>
+int pw_nf(const PwArgs& a, cudaStream_t s) {
+  return a.conf ? pw_go<R, KAHAN, NF, true>(a, s) : pw_go<R, KAHAN, NF, false>(a, s);
+}
+
+// ----------------------------------------------------------- k-space pass
+template <typename R, typename C>
+__global__ void __launch_bounds__(256) kmul_kernel(KmulArgs a) {
+  C* F = static_cast<C*>(a.Fk);
+  const int hx = a.nx / 2 + 1;
+  const int64_t M = (int64_t)hx * a.ny * a.nz;
+  const int64_t tot = M * a.nf;
+  const R dkx2 = (R)a.dkx2, dky2 = (R)a.dky2, dkz2 = (R)a.dkz2, invN = (R)a.invN;
+  using Acc = typename AccOf<R>::type;
+  Acc acc;
+  // 32-bit index arithmetic: nf * M < 2^31 is checked at handle creation
+  const unsigned int stride = gridDim.x * blockDim.x;
+  const unsigned int Mu = (unsigned int)M, hxu = (unsigned int)hx, nyu = (unsigned int)a.ny;
+  for (unsigned int m = blockIdx.x * blockDim.x + threadIdx.x; m < (unsigned int)tot; m += stride) {
+    const unsigned int mm = m % Mu;
+    const int x = (int)(mm % hxu);
+    const unsigned int r = mm / hxu;
+    const int y = (int)(r % nyu), z = (int)(r / nyu);
+    const int jj = fold_idx(y, a.ny), kk = fold_idx(z, a.nz);
+    const R k2 = (R)(x * x) * dkx2 + (R)(jj * jj) * dky2 + (R)(kk * kk) * dkz2;
+    C v = F[m];
+    if (a.store_ge2) {
+      const R w = (x == 0 || 2 * x == a.nx) ? R(1) : R(2);
+      acc.add(w * k2 * (v.x * v.x + v.y * v.y));
+    }
+    const R sc = -k2 * invN;
+    v.x *= sc;
+    v.y *= sc;
+    F[m] = v;
+  }
+  if (a.store_ge2) {
+    double v[1] = {acc.val()}, t[1];
+    if (grid_reduce<1>(v, a.rb, t)) {
+      a.sc->ge2 = t[0] * a.invN;
+      if (bad(t[0])) a.sc->err |= 1u;
+    }
+  }
+}
+
+__global__ void grav_kernel(DevScalars* sc, double h) { sc->a = sc->a - h * sc->ap / 6.0; }
+
+}  // namespace
+
+int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s) {
+  if (a.nf == 1) return precision == LAT_FP64 ? pw_nf<double, false, 1>(a, s) : pw_nf<float, true, 1>(a, s);
+  if (a.nf == 2) return precision == LAT_FP64 ? pw_nf<double, false, 2>(a, s) : pw_nf<float, true, 2>(a, s);
+  return set_error(LAT_ERR_UNSUPPORTED, "pointwise passes support nfld = 1 or 2");
+}
+
+int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
+  if (precision == LAT_FP64) kmul_kernel<double, double2><<<a.grid, a.block, 0, s>>>(a);
+  else kmul_kernel<float, float2><<<a.grid, a.block, 0, s>>>(a);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "kmul launch");
+}
+
+int launch_grav(DevScalars* sc, double h, cudaStream_t s) {
+  grav_kernel<<<1, 1, 0, s>>>(sc, h);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "grav launch");
+}
+
+}  // namespace lat

@@ -1,0 +1,300 @@
+"""GPU engine vs CPU oracle on identical inputs (FP64: <= 1e-10 relative).
+
+Every evolution test starts both sides from the same state, runs the same
+reference call sequence (symp / o2step / Hamiltonian_Split) and compares the
+fields, momenta and Friedmann scalars.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from helpers import L, bubble_fd27, phi4_fd7, two_field_spectral, random_state, vacuum_ic
+
+pytestmark = pytest.mark.gpu
+TOL64 = 1e-10
+
+
+def pair(engine, orc, c):
+    return engine.Lattice(c), orc.Oracle(c)
+
+
+def same_start(g, o, seed=1, mean=1.0, amp=0.05):
+    f, p = random_state((g.nfld, g.nz, g.ny, g.nx), seed=seed, mean=mean, amp=amp)
+    g.set_state(f, p)
+    o.set_state(f, p)
+    return f, p
+
+
+def compare_state(g, o, tol=TOL64):
+    gf, gp = g.get_state()
+    of, op = o.get_state()
+    assert rel_err(gf, of) <= tol, rel_err(gf, of)
+    assert rel_err(gp, op) <= tol, rel_err(gp, op)
+
+
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
+def test_fd7_minkowski_symp(engine, orc, order):
+    c = phi4_fd7(16)
+    g, o = pair(engine, orc, c)
+    same_start(g, o)
+    dt = c.len / c.nx / 10
+    g.symp(order, dt, 5)
+    o.symp(order, dt, 5)
+    compare_state(g, o)
+    assert np.allclose(g.time(), o.time(), rtol=0, atol=1e-15)
+
+
+def test_fd7_64cube_100_steps(engine, orc):
+    """The 64^3 plain-method workload (L=20, dt=dx/10, phi^4, FD7, leapfrog), 100 steps."""
+    c = phi4_fd7(64)
+    g, o = pair(engine, orc, c)
+    vacuum_ic(g, seed=1000, amp=1e-8)
+    vacuum_ic(o, seed=1000, amp=1e-8)
+    compare_state(g, o, 1e-12)
+    dt = (20.0 / 64) / 10
+    for _ in range(10):
+        g.symp(2, dt, 10)
+        o.symp(2, dt, 10)
+    compare_state(g, o)
+    eg, eo = g.energies(), o.energies()
+    assert abs(eg[L.E_RHO] - eo[L.E_RHO]) <= 1e-10 * abs(eo[L.E_RHO])
+
+
+@pytest.mark.parametrize("split", [L.SPLIT_PSEUDOSPEC, L.SPLIT_DEFROST])
+def test_fd27_gw_minkowski(engine, orc, split):
+    c = bubble_fd27(16, split=split)
+    g, o = pair(engine, orc, c)
+    same_start(g, o, mean=0.0, amp=0.3)
+    dt = 0.25 / 10
+    g.symp(2, dt, 12)
+    o.symp(2, dt, 12)
+    compare_state(g, o)
+    gu, gpu_ = g.gw_state()
+    ou, opu = o.gw_state()
+    assert rel_err(gu, ou) <= TOL64
+    assert rel_err(gpu_, opu) <= TOL64
+    Sg, Wg = g.gw_spectrum(16)
+    So, Wo = o.gw_spectrum(16)
+    assert np.array_equal(Wg, Wo)
+    assert rel_err(Sg, So) <= 1e-9
+
+
+def test_fd27_conformal_plain_path(engine, orc):
+    c = L.make_config(16, nfld=2, length=8.0, laplacian=L.LAP_FD27, background=L.BG_CONFORMAL,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g, o = pair(engine, orc, c)
+    same_start(g, o)
+    g.calc_metric()
+    o.calc_metric()
+    assert abs(g.scale_factor()[1] - o.scale_factor()[1]) <= 1e-12 * abs(o.scale_factor()[1])
+    g.symp(4, 0.05, 6)
+    o.symp(4, 0.05, 6)
+    compare_state(g, o)
+    (ag, apg), (ao, apo) = g.scale_factor(), o.scale_factor()
+    assert abs(ag - ao) <= 1e-12 * ao and abs(apg - apo) <= 1e-10 * abs(apo)
+
+
+@pytest.mark.parametrize("conformal", [False, True])
+def test_spectral_two_field_fused(engine, orc, conformal):
+    c = two_field_spectral(32, conformal=conformal)
+    g, o = pair(engine, orc, c)
+    vacuum_ic(g, amp=1e-3)
+    vacuum_ic(o, amp=1e-3)
+    if conformal:
+        g.calc_metric()
+        o.calc_metric()
+    dt = c.len / c.nx / 20
+    for _ in range(4):
+        g.symp(4, dt, 5)
+        o.symp(4, dt, 5)
+    compare_state(g, o)
+    if conformal:
+        (ag, apg), (ao, apo) = g.scale_factor(), o.scale_factor()
+        assert abs(ag - ao) <= 1e-12 * ao
+        assert abs(apg - apo) <= 1e-10 * abs(apo)
+
+
+def test_spectral_o2step_and_split(engine, orc):
+    c = two_field_spectral(16, conformal=True)
+    g, o = pair(engine, orc, c)
+    same_start(g, o, amp=0.02)
+    for obj in (g, o):
+        obj.set_scale_factor(1.0, -0.5)
+        obj.hamiltonian_split(0.01, 1)
+        obj.o2step(0.02, 0.6, 0.4)
+        obj.hamiltonian_split(0.03, 3)
+        obj.hamiltonian_split(0.01, 2)
+    compare_state(g, o)
+    assert np.allclose(g.scale_factor(), o.scale_factor(), rtol=1e-12, atol=0)
+    assert np.allclose(g.time(), o.time(), rtol=0, atol=1e-15)
+
+
+def test_laplacians(engine, orc):
+    for c in (two_field_spectral(16, conformal=False), phi4_fd7(16),
+              L.make_config((16, 12, 10), nfld=1, length=5.0, laplacian=L.LAP_FD27)):
+        g, o = pair(engine, orc, c)
+        same_start(g, o)
+        assert rel_err(g.laplacian(0), o.laplacian(0)) <= 1e-12
+
+
+def test_standalone_laplacian_3d(engine):
+    n1, n2, n3 = 16, 12, 8
+    dk = 0.7
+    x = np.arange(n1)[None, None, :]
+    y = np.arange(n2)[None, :, None]
+    f = np.cos(2 * np.pi * 3 * x / n1) * np.sin(2 * np.pi * 2 * y / n2) + 0 * np.zeros((n3, 1, 1))
+    lap = engine.laplacian_3d(f, dk)
+    expect = -((3 * dk) ** 2 + (2 * dk) ** 2) * f
+    assert np.max(np.abs(lap - expect)) <= 1e-12 * np.max(np.abs(expect))
+
+
+def test_vacuum_ic_identical(engine, orc):
+    c = two_field_spectral(32)
+    g, o = pair(engine, orc, c)
+    vacuum_ic(g, seed=1001, amp=1e-8)
+    vacuum_ic(o, seed=1001, amp=1e-8)
+    compare_state(g, o, 1e-12)
+
+
+def test_energies(engine, orc):
+    for c in (phi4_fd7(16), bubble_fd27(12), two_field_spectral(16, conformal=True)):
+        g, o = pair(engine, orc, c)
+        same_start(g, o)
+        if c.background == L.BG_CONFORMAL:
+            g.set_scale_factor(1.3, -0.7)
+            o.set_scale_factor(1.3, -0.7)
+        eg, eo = g.energies(), o.energies()
+        for i in range(L.NENERGY):
+            assert abs(eg[i] - eo[i]) <= 1e-10 * max(abs(eo[i]), 1e-300), (i, eg[i], eo[i])
+        assert abs(eg[L.E_GE_LAP] - eg[L.E_GE_GRAD]) <= 1e-10 * abs(eg[L.E_GE_LAP])
+
+
+def test_spectra_modes_exact(engine, orc):
+    c = two_field_spectral(24, conformal=False)
+    g, o = pair(engine, orc, c)
+    same_start(g, o)
+    for what in (L.SPEC_FLD, L.SPEC_FLDP):
+        for mode in (L.SPEC_WEIGHTED, L.SPEC_COUNT):
+            Sg, Wg = g.spectrum(what, 1, mode)
+            So, Wo = o.spectrum(what, 1, mode)
+            if mode == L.SPEC_COUNT:
+                assert np.array_equal(Wg, Wo)  # bit-exact integer mode counts
+            else:
+                assert rel_err(Wg, Wo) <= 1e-13
+            assert rel_err(Sg, So) <= 1e-11
+    Srg, Sig = g.crossspec_3d(L.SPEC_FLD, 0, L.SPEC_FLDP, 1)
+    Sro, Sio = o.crossspec_3d(L.SPEC_FLD, 0, L.SPEC_FLDP, 1)
+    assert rel_err(Srg, Sro) <= 1e-11 and rel_err(Sig, Sio) <= 1e-11
+
+
+def test_standalone_spectrum_3d(engine, orc):
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((10, 12, 16))
+    c = L.make_config((16, 12, 10), nfld=1, length=1.0)
+    o = orc.Oracle(c)
+    o.set_state(f[None])
+    for mode in (L.SPEC_WEIGHTED, L.SPEC_COUNT):
+        Sg, Wg = engine.spectrum_3d(f, mode)
+        So, Wo = o.spectrum(0, 0, mode)
+        assert rel_err(Sg, So) <= 1e-12
+        if mode == L.SPEC_COUNT:
+            assert np.array_equal(Wg, Wo)
+
+
+def test_bubbles_ic(engine, orc):
+    c = bubble_fd27(32, gw=False)
+    g, o = pair(engine, orc, c)
+    cen = [[4.0, 4.0, 4.0], [4.0 + 2.5, 4.0, 4.0]]
+    g.init_bubbles(cen, 1.5, math.sqrt(2))
+    o.init_bubbles(cen, 1.5, math.sqrt(2))
+    compare_state(g, o, 1e-13)
+
+
+def test_fortran_layout_padding(engine):
+    c = phi4_fd7(8)
+    c.nfld = 2
+    c.model = L.MODEL_PHI4_G2
+    g = engine.Lattice(c)
+    n = 8
+    rng = np.random.default_rng(5)
+    # DEFROST padding: 2 low, 3 high ghost sites per side (latpar.f90:78-80)
+    lo, hi = 2, 3
+    m = n + lo + hi
+    fld = rng.standard_normal((m, m, m, 2))
+    fldp = rng.standard_normal((n, n, n, 2))
+    g.upload_fortran(fld, lo, hi, fldp, 0, 0)
+    f, p = g.get_state()
+    inner = fld[lo:lo + n, lo:lo + n, lo:lo + n, :]
+    assert np.array_equal(f, np.moveaxis(inner, -1, 0))
+    assert np.array_equal(p, np.moveaxis(fldp, -1, 0))
+    back = np.full_like(fld, -7.0)
+    backp = np.zeros_like(fldp)
+    g.download_fortran(back, lo, hi, backp, 0, 0)
+    assert np.array_equal(back[lo:lo + n, lo:lo + n, lo:lo + n, :], inner)
+    mask = np.ones(back.shape, bool)
+    mask[lo:lo + n, lo:lo + n, lo:lo + n, :] = False
+    assert np.all(back[mask] == -7.0)  # ghost sites untouched
+
+
+def test_checkpoint_roundtrip(engine, tmp_path):
+    c = two_field_spectral(16, conformal=True)
+    g = engine.Lattice(c)
+    vacuum_ic(g, amp=1e-3)
+    g.set_scale_factor(1.25, -0.75)
+    g.checkpoint_write(tmp_path, 3.5, 7)
+    f, p = g.get_state()
+    h = engine.Lattice(c)
+    t, fr = h.checkpoint_read(tmp_path)
+    assert (t, fr) == (3.5, 7)
+    f2, p2 = h.get_state()
+    assert np.array_equal(f, f2) and np.array_equal(p, p2)
+    assert h.scale_factor() == (1.25, -0.75)
+    raw = np.fromfile(tmp_path / "fld_2.raw")
+    assert np.array_equal(raw.reshape(16, 16, 16), f[1])
+
+
+def test_checkpoint_corrupt_header(engine, tmp_path):
+    c = phi4_fd7(8)
+    g = engine.Lattice(c)
+    g.checkpoint_write(tmp_path)
+    (tmp_path / "checkpt.dat").write_text("garbage\n")
+    with pytest.raises(engine.LatticeError) as e:
+        g.checkpoint_read(tmp_path)
+    assert e.value.code == 7
+    (tmp_path / "fld_1.raw").write_bytes(b"\0" * 100)
+    with pytest.raises(engine.LatticeError):
+        g.checkpoint_read(tmp_path)
+
+
+def test_deterministic_reductions(engine):
+    c = two_field_spectral(32, conformal=True)
+    outs = []
+    for _ in range(2):
+        g = engine.Lattice(c)
+        vacuum_ic(g, amp=1e-3)
+        g.calc_metric()
+        g.symp(4, 0.01, 10)
+        outs.append((g.get_state(), g.scale_factor()))
+    (f1, p1), s1 = outs[0]
+    (f2, p2), s2 = outs[1]
+    assert np.array_equal(f1, f2) and np.array_equal(p1, p2) and s1 == s2
+
+
+def test_graph_replay_matches_eager(engine, monkeypatch):
+    c = phi4_fd7(16)
+    g = engine.Lattice(c)
+    f, p = random_state((1, 16, 16, 16), seed=9)
+    g.set_state(f, p)
+    for _ in range(3):
+        g.symp(2, 0.03, 3)  # first call captures a graph, later calls replay it
+    a = g.get_state()
+    g.timing(True)  # timing disables graphs: eager launches
+    g.set_state(f, p)
+    for _ in range(3):
+        g.symp(2, 0.03, 3)
+    b = g.get_state()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
