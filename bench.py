@@ -52,6 +52,7 @@ def workload_config(L, precision, n=N_SIDE):
 
 def init_state(obj, seed):
     obj.init_vacuum(seed, [1.0, 0.0], [0.0, 0.0], [3.0, 2.0], amp=1e-8, kcut_frac=0.5)
+    obj.set_scale_factor(1.0, 0.0)  # a(0) = 1, then ysclp from the Friedmann constraint
     obj.calc_metric()
 
 
@@ -79,7 +80,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -183,7 +184,7 @@ def run_reference(args):
     budget = float(os.environ.get("LAT_REF_BUDGET_S", "60"))
     rate, cores, done, el = cpu_rate(steps_budget_s=budget, max_steps=max(args.steps, 1))
     line = {
-        "impl": "reference", "metric": METRIC.replace("FP32-Kahan", "FP64 CPU"), "value": rate, "unit": UNIT,
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": ws, "steps": done, "warmup": 1, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vacuum fluctuations)",
         "config": {"workload": "two-field preheating 256^3, L=10pi, spectral, Yoshida-4, conformal, dt=dx/20",
@@ -379,7 +380,7 @@ def diagnostics(L, g, args, dt, ms_step):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-sub", type=int, default=10)

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "integrator.hpp"
 
 namespace lat {
 
@@ -61,11 +62,6 @@ using namespace lat;
   } while (0)
 
 namespace {
-
-struct Op {
-  char t;    // 'D' drift, 'K' kick, 'G' gravity kinetic, 'M' metric kinetic (Minkowski no-op)
-  double h;
-};
 
 struct GraphEntry {
   int order;
@@ -303,83 +299,9 @@ int spectral_lap(lat_s* h, bool store_ge2) {
 }
 
 // ------------------------------------------------------------ op lists
-struct Emitter {
-  lat_s* h;
-  std::vector<Op>* ops;
-  double* tg;
-  int split(double dt, int hamind) {
-    if (hamind < 1 || hamind > n_terms(h)) return set_error(LAT_ERR_ARG, "Undefined Hamiltonian term");
-    tg[hamind - 1] += dt;
-    const bool conf = conformal(h);
-    if (h->cfg.split_order == LAT_SPLIT_DEFROST) {
-      if (hamind == 1) ops->push_back({conf ? 'G' : 'M', dt});
-      else if (hamind == 2) ops->push_back({'D', dt});
-      else ops->push_back({'K', dt});
-    } else {
-      if (hamind == 1) ops->push_back({'D', dt});
-      else if (hamind == n_terms(h)) ops->push_back({'K', dt});
-      else ops->push_back({'G', dt});
-    }
-    return LAT_OK;
-  }
-  int o2step(double dt, double w1, double w2) {
-    const int nt = n_terms(h);
-    for (int i = 2; i <= nt - 1; ++i) RET(split(w1 * dt / 2.0, i));
-    RET(split(w1 * dt, nt));
-    for (int i = nt - 1; i >= 2; --i) RET(split(w1 * dt / 2.0, i));
-    return split((w1 + w2) * dt / 2.0, 1);
-  }
-  // symp2/4/6/8 of evolve_spectral.f90:129-227 (DEFROST: evolve.f90:118-223)
-  int symp(int order, double dt, int nsteps) {
-    const bool df = h->cfg.split_order == LAT_SPLIT_DEFROST;
-    if (nsteps < 1) return set_error(LAT_ERR_ARG, "nsteps < 1");
-    if (order == 2) {
-      RET(split(dt / 2.0, 1));
-      for (int j = 1; j <= nsteps - 1; ++j) RET(o2step(dt, 1.0, 1.0));
-      return o2step(dt, 1.0, 0.0);
-    }
-    if (order == 4) {
-      const double w1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0));
-      const double w0 = 1.0 - 2.0 * w1;
-      RET(split(w1 * dt / 2.0, 1));
-      for (int j = 1; j <= nsteps; ++j) {
-        RET(o2step(dt, w1, w0));
-        RET(o2step(dt, w0, w1));
-        RET(o2step(dt, w1, j == nsteps ? 0.0 : w1));
-      }
-      return LAT_OK;
-    }
-    if (order == 6) {
-      const double w3 = 0.784513610477560, w2 = 0.235573213359357;
-      const double w1 = df ? -1.17767998417887 : -1.177679984177887;
-      const double w0 = 1.0 - 2.0 * (w1 + w2 + w3);
-      RET(split(w3 * dt / 2.0, 1));
-      for (int j = 1; j <= nsteps; ++j) {
-        RET(o2step(dt, w3, w2)); RET(o2step(dt, w2, w1)); RET(o2step(dt, w1, w0));
-        RET(o2step(dt, w0, w1)); RET(o2step(dt, w1, w2)); RET(o2step(dt, w2, w3));
-        RET(o2step(dt, w3, j == nsteps ? 0.0 : w3));
-      }
-      return LAT_OK;
-    }
-    if (order == 8) {
-      if (df) return set_error(LAT_ERR_UNSUPPORTED, "the DEFROST symp8 has no coefficients (evolve.f90:180-188)");
-      const double w[8] = {0, 0.74167036435061295344822780, -0.40910082580003159399730010,
-                           0.19075471029623837995387626, -0.57386247111608226665638733,
-                           0.29906418130365592384446354, 0.33462491824529818378495798,
-                           0.31529309239676659663205666};
-      const double w0 = 1.0 - 2.0 * (w[1] + w[2] + w[3] + w[4] + w[5] + w[6] + w[7]);
-      const double W[8] = {w0, w[1], w[2], w[3], w[4], w[5], w[6], w[7]};
-      RET(split(W[7] * dt / 2.0, 1));
-      for (int j = 1; j <= nsteps; ++j) {
-        for (int i = 7; i >= 1; --i) RET(o2step(dt, W[i], W[i - 1]));
-        for (int i = 0; i <= 6; ++i) RET(o2step(dt, W[i], W[i + 1]));
-        RET(o2step(dt, W[7], j == nsteps ? 0.0 : W[7]));
-      }
-      return LAT_OK;
-    }
-    return set_error(LAT_ERR_ARG, "order must be 2, 4, 6 or 8");
-  }
-};
+Emitter emitter(lat_s* h, std::vector<Op>* ops, double* tg) {
+  return Emitter{n_terms(h), h->cfg.split_order == LAT_SPLIT_DEFROST, conformal(h), ops, tg};
+}
 
 // ----------------------------------------------------------- execution
 int exec_drift(lat_s* h, double hd) {
@@ -841,7 +763,7 @@ int lat_split(lat_t* h, double dt, int32_t hamind) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   std::vector<Op> ops;
-  Emitter em{h, &ops, h->tglobal};
+  Emitter em = emitter(h, &ops, h->tglobal);
   RET(em.split(dt, hamind));
   return exec_plain(h, ops);
 }
@@ -850,7 +772,7 @@ int lat_o2step(lat_t* h, double dt, double w1, double w2) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   std::vector<Op> ops;
-  Emitter em{h, &ops, h->tglobal};
+  Emitter em = emitter(h, &ops, h->tglobal);
   RET(em.o2step(dt, w1, w2));
   return exec_plain(h, ops);
 }
@@ -860,7 +782,7 @@ int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps) {
   ApiGuard g(h);
   std::vector<Op> ops;
   double tg[3] = {h->tglobal[0], h->tglobal[1], h->tglobal[2]};
-  Emitter em{h, &ops, tg};
+  Emitter em = emitter(h, &ops, tg);
   RET(em.symp(order, dt, nsteps));
   const bool graphs = h->use_graphs && !h->timing;
   if (!graphs) {
@@ -1304,6 +1226,164 @@ int lat_spectrum_3d(int32_t n1, int32_t n2, int32_t n3, const double* f, int32_t
   if (st == LAT_OK) st = lat_spectrum(h, LAT_SPEC_FLD, 0, mode, nbins, S, W);
   lat_destroy(h);
   return st;
+}
+
+// ------------------------------------------------------------- autotune
+namespace {
+
+std::string tune_key(lat_s* h) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, h->dev);
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s|sm%d%d|p%d|lap%d|bg%d|nf%d|gw%d|%dx%dx%d", prop.name, prop.major, prop.minor,
+           h->prec, h->cfg.laplacian, h->cfg.background, h->nf, h->cfg.gw, h->nx, h->ny, h->nz);
+  return buf;
+}
+
+bool tune_lookup(const char* path, const std::string& key, int v[4]) {
+  if (!path) return false;
+  FILE* fp = fopen(path, "r");
+  if (!fp) return false;
+  char line[1024];
+  bool found = false;
+  const std::string pat = "\"key\": \"" + key + "\"";
+  while (fgets(line, sizeof(line), fp)) {
+    if (!strstr(line, pat.c_str())) continue;
+    int a, b, c, d;
+    const char* q = strstr(line, "\"ty\":");
+    if (q && sscanf(q, "\"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d", &a, &b, &c, &d) == 4) {
+      v[0] = a; v[1] = b; v[2] = c; v[3] = d;
+      found = true;
+    }
+  }
+  fclose(fp);
+  return found;
+}
+
+// device time of `reps` executions of one representative pass
+int time_pass(lat_s* h, int reps, float* ms) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  int st = LAT_OK;
+  const double hk = 1e-3, hg = 5e-4, hd = 1e-3;
+  for (int w = 0; w < 2 && st == LAT_OK; ++w) {  // w = 0 warms up
+    cudaEventRecord(a, h->stream);
+    for (int r = 0; r < reps && st == LAT_OK; ++r) {
+      if (spectral(h) || !conformal(h)) st = exec_kd(h, hk, conformal(h) ? hg : 0.0, hd);
+      else st = exec_kick(h, hk);
+    }
+    cudaEventRecord(b, h->stream);
+  }
+  if (st == LAT_OK) {
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(ms, a, b);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return st;
+}
+
+}  // namespace
+
+int lat_autotune(lat_t* h, const char* cache_path) {
+  if (!h) return set_error(LAT_ERR_ARG, "null handle");
+  ApiGuard g(h);
+  const std::string key = tune_key(h);
+  int v[4];
+  if (tune_lookup(cache_path, key, v)) {
+    h->fd_ty = v[0]; h->fd_zc = std::min(v[1], h->nz); h->pw_block = v[2]; h->pw_grid = h->nsm * v[3];
+    free_graphs(h);
+    return LAT_OK;
+  }
+  // save the state: candidates run real passes on this lattice
+  const size_t fb = (size_t)h->nf * h->N * h->rsz, gb = (size_t)6 * h->N * h->rsz;
+  std::vector<void*> saved;
+  auto save = [&](void* src, size_t bytes) -> int {
+    void* d = nullptr;
+    if (!src) { saved.push_back(nullptr); return LAT_OK; }
+    CK(cudaMalloc(&d, bytes));
+    CK(cudaMemcpyAsync(d, src, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    saved.push_back(d);
+    return LAT_OK;
+  };
+  const int cur0 = h->cur, ucur0 = h->ucur;
+  RET(save(h->fld[h->cur], fb));
+  RET(save(h->fldc, fb));
+  RET(save(h->fldp, fb));
+  RET(save(h->cfg.gw ? h->u[h->ucur] : nullptr, gb));
+  RET(save(h->cfg.gw ? h->pu : nullptr, gb));
+  RET(save(h->sc, sizeof(DevScalars)));
+  const bool was_timing = h->timing;
+  h->timing = false;
+  int st = LAT_OK;
+  float best = 1e30f;
+  int bty = h->fd_ty, bzc = h->fd_zc, bpb = h->pw_block, bbps = h->pw_grid / h->nsm;
+  const int reps = h->N >= (1 << 22) ? 3 : 10;
+  if (!spectral(h)) {
+    for (int ty : {2, 4, 8, 16})
+      for (int zc : {8, 16, 32, 64}) {
+        if (st != LAT_OK) break;
+        if (zc > h->nz && zc != 8) continue;
+        h->fd_ty = ty;
+        h->fd_zc = std::min(zc, h->nz);
+        float ms = 0;
+        st = time_pass(h, reps, &ms);
+        if (st == LAT_OK && ms < best) { best = ms; bty = ty; bzc = h->fd_zc; }
+      }
+    h->fd_ty = bty;
+    h->fd_zc = bzc;
+  }
+  best = 1e30f;
+  for (int pb : {128, 256})
+    for (int bps : {1, 2, 4, 8}) {
+      if (st != LAT_OK) break;
+      if ((int64_t)h->nsm * bps > h->red_cap) continue;
+      h->pw_block = pb;
+      h->pw_grid = h->nsm * bps;
+      float ms = 0;
+      if (!spectral(h) && !conformal(h)) {  // FD Minkowski: the pointwise drift is the only pointwise pass
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        exec_drift(h, 1e-3);
+        cudaEventRecord(a, h->stream);
+        for (int r = 0; r < reps; ++r) st = exec_drift(h, 1e-3);
+        cudaEventRecord(b, h->stream);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+      } else {
+        st = time_pass(h, reps, &ms);
+      }
+      if (st == LAT_OK && ms < best) { best = ms; bpb = pb; bbps = bps; }
+    }
+  h->pw_block = bpb;
+  h->pw_grid = h->nsm * bbps;
+  h->timing = was_timing;
+  // restore
+  h->cur = cur0;
+  h->ucur = ucur0;
+  void* dst[6] = {h->fld[h->cur], h->fldc, h->fldp, h->cfg.gw ? h->u[h->ucur] : nullptr,
+                  h->cfg.gw ? h->pu : nullptr, h->sc};
+  size_t sz[6] = {fb, fb, fb, gb, gb, sizeof(DevScalars)};
+  for (int i = 0; i < 6; ++i)
+    if (saved[i]) cudaMemcpyAsync(dst[i], saved[i], sz[i], cudaMemcpyDeviceToDevice, h->stream);
+  CK(cudaStreamSynchronize(h->stream));
+  for (void* p : saved)
+    if (p) cudaFree(p);
+  free_graphs(h);
+  if (st != LAT_OK) return st;
+  if (cache_path) {
+    FILE* fp = fopen(cache_path, "a");
+    if (fp) {
+      fprintf(fp, "{\"key\": \"%s\", \"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d}\n", key.c_str(),
+              h->fd_ty, h->fd_zc, h->pw_block, h->pw_grid / h->nsm);
+      fclose(fp);
+    }
+  }
+  return LAT_OK;
 }
 
 int lat_tuning_get(const lat_t* h, int32_t out[5]) {
