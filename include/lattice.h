@@ -190,6 +190,22 @@ int lat_crossspec(lat_t* h, int32_t what1, int32_t field1, int32_t what2,
 /* Stand-alone spectrum_3d(S,f,Fk,plan) of a host array f(n1,n2,n3). */
 int lat_spectrum_3d(int32_t n1, int32_t n2, int32_t n3, const double* f,
                     int32_t mode, int32_t nbins, double* S, double* W);
+/* Binning of a half spectrum already on the device, allocating nothing.
+ * No counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc -- a driver that has given the whole device to its own fixed
+ * memory pool, or a code that must not allocate once its time loop runs.
+ * Fk_dev: half spectrum [nz][ny][nx/2+1] of complex FP64 (precision
+ * LAT_FP64) or FP32 (LAT_FP32_KAHAN), as written by lat_spectrum's R2C;
+ * out_dev: 2*nbins doubles on the device, S(l) = sum c|F|^2 / W(l) then W(l);
+ * mode as lat_spectrum; stream: a cudaStream_t or NULL for the default stream.
+ * Scratch is a fixed 1 MiB static device array that every GPU loading this
+ * library keeps until exit; nbins above 512 is rejected with LAT_ERR_ARG.
+ * All calls share that scratch: calls that overlap on the GPU race, so order
+ * them.  The first call on a device looks up the scratch's device address
+ * (with that device current); make it before any stream capture. */
+int lat_spectrum_noalloc(const void* Fk_dev, int32_t nx, int32_t ny, int32_t nz,
+                         int32_t precision, int32_t mode, int32_t nbins,
+                         double* out_dev, void* stream);
 
 /* ---------------------------------------------------- gravitational waves */
 /* TT-projected GW spectrum: sum over modes of sum_ij |Lambda_ij,lm pi_lm(k)|^2

@@ -97,6 +97,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_energies": ([P, dp], I), "lat_spectrum_nbins": ([P, C.POINTER(I)], I),
         "lat_spectrum": ([P, I, I, I, I, dp, dp], I), "lat_crossspec": ([P, I, I, I, I, I, dp, dp], I),
         "lat_spectrum_3d": ([I, I, I, dp, I, I, dp, dp], I),
+        "lat_spectrum_noalloc": ([P, I, I, I, I, I, I, P, P], I),
         "lat_gw_spectrum": ([P, I, dp, dp], I), "lat_gw_download": ([P, dp, dp], I),
         "lat_gw_upload": ([P, dp, dp], I),
         "lat_init_vacuum": ([P, U64, dp, dp, dp, D, D], I), "lat_init_bubbles": ([P, I, dp, D, D], I),
