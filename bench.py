@@ -45,9 +45,9 @@ N_SIDE = 256
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 
 
-def workload_config(L, precision, n=N_SIDE):
+def workload_config(L, precision, n=N_SIDE, impl=0):
     return L.make_config(n, nfld=2, length=10 * math.pi, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
-                         precision=precision, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+                         precision=precision, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0), spectral_impl=impl)
 
 
 def init_state(obj, seed):
@@ -205,13 +205,21 @@ def run_ours(args):
     L = importlib.import_module("lattice-dev_gb300")
     L.load_library()
     K, W = args.steps, args.warmup
-    c = workload_config(L, L.FP32_KAHAN)
+    if args.case == "fd-bubbles":
+        return run_fd_case(L, args, local)
+    n = args.n
+    impl = {"auto": L.SPEC_IMPL_AUTO, "cufft": L.SPEC_IMPL_CUFFT, "separable": L.SPEC_IMPL_SEPARABLE}[args.spectral_impl]
+    c = workload_config(L, L.FP32_KAHAN, n, impl)
     c.device = local
     g = L.Lattice(c)
-    n = N_SIDE
     N = n ** 3
     dt = c.len / n / 20
     init_state(g, 1000 + rank)
+    # tile shapes, launch shapes and (with spectral_impl auto) the spectral path
+    # picked by the autotuner on this lattice; the state is restored afterwards
+    if not args.no_autotune:
+        g.autotune(os.environ.get("LAT_TUNE_CACHE"))
+    tuning = g.tuning()
 
     # warm-up
     g.symp(4, dt, W)
@@ -235,7 +243,7 @@ def run_ours(args):
     value = ws * N * K / (ms * 1e-3)
 
     extra = {}
-    if rank == 0 and not args.quick:
+    if rank == 0 and not args.quick and n == N_SIDE:
         extra = diagnostics(L, g, args, dt, ms / K)
     g.close()
 
@@ -243,13 +251,17 @@ def run_ours(args):
         return 0
     pk, pk_kind = peaks()
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "metric": METRIC if n == N_SIDE else METRIC.replace("256^3", f"{n}^3"),
+        "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (Kahan-compensated drifts, f64 reductions)",
         "data": "synthetic (seeded vacuum fluctuations, 1e-8/(2w_k) spectrum)",
-        "config": {"workload": "two-field preheating 256^3, L=10pi, spectral, Yoshida-4, conformal, dt=dx/20",
+        "config": {"workload": f"two-field preheating {n}^3, L=10pi, spectral, Yoshida-4, conformal, dt=dx/20",
                    "global_batch": N * ws, "seq_len": 1, "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (state 403 MB + spectra 270 MB per replica)"},
+                   "l2": "inputs larger than L2 (state 403 MB + spectra 270 MB per replica)"
+                         if n == N_SIDE else "small profiling case",
+                   "tuning": list(tuning),
+                   "spectral_path": "separable passes" if tuning[5] == L.SPEC_IMPL_SEPARABLE else "cuFFT 3D"},
         "clocks": clocks, "gpu_launches": launches,
     }
     line.update(extra)
@@ -273,7 +285,8 @@ def diagnostics(L, g, args, dt, ms_step):
     g.sync()
     cls = {}
     names = {L.K_KICKDRIFT: "kickdrift", L.K_DRIFT: "drift", L.K_KICK: "kick", L.K_KMUL: "kmul",
-             L.K_FFT_R2C: "cufft_r2c", L.K_FFT_C2R: "cufft_c2r", L.K_OTHER: "other"}
+             L.K_FFT_R2C: "cufft_r2c", L.K_FFT_C2R: "cufft_c2r", L.K_OTHER: "other",
+             L.K_SEP_X: "sep_x", L.K_SEP_Y: "sep_y", L.K_SEP_Z: "sep_z"}
     for k, nm in names.items():
         t, nl = g.timing_read(k)
         if nl:
@@ -284,8 +297,9 @@ def diagnostics(L, g, args, dt, ms_step):
         v["share"] = v["ms"] / tot
     out["kernel_classes"] = cls
     # algorithmic bytes per launch of the engine kernels (2 fields)
+    # per launch, two FP32 fields: X r phi,c,pi w phi,c,lap; Y r phi,c,lap w lap; Z r phi,c,lap,pi w pi
     bytes_per = {"kickdrift": 2 * 28 * N, "kmul": 2 * 2 * 8 * (n // 2 + 1) * n * n,
-                 "drift": 2 * 20 * N}
+                 "drift": 2 * 20 * N, "sep_x": 2 * 24 * N, "sep_y": 2 * 16 * N, "sep_z": 2 * 20 * N}
     own = {k: v for k, v in cls.items() if k in bytes_per}
     if own:
         dom = max(own, key=lambda k: own[k]["ms"])
@@ -294,11 +308,31 @@ def diagnostics(L, g, args, dt, ms_step):
         out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                            "frac": ach / hbm, "traffic": None,
                            "algorithmic_bytes_per_launch": bytes_per[dom]}
-    # whole step against the fused byte model (264.4 B per site-update)
+    # whole step against the byte model of a 3D-FFT design (264.4 B per site-update) and against the
+    # bytes the separable passes actually move (3 kicks x 2 fields x 60 B)
     step_bytes = 3 * (2 * (2 * 4 * N + 2 * 8 * (n // 2 + 1) * n * n) + 2 * 28 * N)
-    out["step_roofline"] = {"bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (ms_step * 1e-3) / 1e9,
-                            "frac": step_bytes / (ms_step * 1e-3) / 1e9 / hbm,
-                            "model": "3 x (2 FFT r2c+c2r I/O + 28 B/site/field fused kick-drift)"}
+    sep_bytes = 3 * 2 * 60 * N
+    out["step_roofline"] = {"bytes_per_step_fft_model": step_bytes,
+                            "frac_fft_model": step_bytes / (ms_step * 1e-3) / 1e9 / hbm,
+                            "bytes_per_step_separable": sep_bytes,
+                            "achieved_gbs_separable": sep_bytes / (ms_step * 1e-3) / 1e9,
+                            "frac_separable": sep_bytes / (ms_step * 1e-3) / 1e9 / hbm,
+                            "model": "fft: 3 x (2 FFT r2c+c2r I/O + 28 B/site/field); separable: 3 x 2 x (24+16+20) B/site"}
+    # ---- both spectral paths: step time and FP32 accuracy
+    paths = {}
+    for impl, name in ((L.SPEC_IMPL_CUFFT, "cufft"), (L.SPEC_IMPL_SEPARABLE, "separable")):
+        gp = L.Lattice(workload_config(L, L.FP32_KAHAN, impl=impl))
+        init_state(gp, 1000)
+        gp.symp(4, dt, 3)
+        Kp = max(10, args.steps // 4)
+        gp.sync()
+        gp.mark(0)
+        gp.symp(4, dt, Kp)
+        gp.mark(1)
+        msp = gp.mark_elapsed(0, 1) / Kp
+        paths[name] = {"ms_per_step": msp, "value": N / (msp * 1e-3)}
+        gp.close()
+    out["spectral_paths"] = paths
     # ---- FP64 plain step on the GPU
     if not args.no_fp64:
         c64 = workload_config(L, L.FP64)
@@ -313,31 +347,35 @@ def diagnostics(L, g, args, dt, ms_step):
         ms64 = g64.mark_elapsed(0, 1) / K64
         out["fp64_plain"] = {"ms_per_step": ms64, "value": N / (ms64 * 1e-3), "steps": K64,
                              "fp32_kahan_speedup": ms64 / ms_step}
-        # ---- accuracy of FP32-Kahan against the FP64 GPU run from the same IC
+        # ---- accuracy of FP32-Kahan (both spectral paths) against the FP64 GPU run from the same IC
         steps_acc = args.acc_steps
-        c32 = workload_config(L, L.FP32_KAHAN)
-        a32 = L.Lattice(c32)
         b64 = g64
-        for obj in (a32, b64):
-            init_state(obj, 4242)
+        init_state(b64, 4242)
         e0 = b64.energies()
-        a32.symp(4, dt, steps_acc)
         b64.symp(4, dt, steps_acc)
-        e32, e64 = a32.energies(), b64.energies()
+        e64 = b64.energies()
         nb = 128
-        acc = {"steps": steps_acc}
-        for f in (0, 1):
-            S32, _ = a32.spectrum(L.SPEC_FLD, f, L.SPEC_WEIGHTED, nb)
-            S64, _ = b64.spectrum(L.SPEC_FLD, f, L.SPEC_WEIGHTED, nb)
-            live = np.arange(nb) >= 1
-            rel = np.abs(S32[live] - S64[live]) / np.maximum(np.abs(S64[live]), 1e-300)
-            acc[f"pk_field{f}_max_rel_err"] = float(np.max(rel[: n // 4]))
-        acc["a_rel_err"] = abs(e32[L.E_A] - e64[L.E_A]) / e64[L.E_A]
-        acc["friedmann_residual_fp32"] = float(e32[L.E_RESIDUAL])
-        acc["friedmann_residual_fp64"] = float(e64[L.E_RESIDUAL])
-        acc["friedmann_residual_initial"] = float(e0[L.E_RESIDUAL])
-        out["accuracy_vs_fp64_gpu"] = acc
-        a32.close()
+        S64 = [b64.spectrum(L.SPEC_FLD, f, L.SPEC_WEIGHTED, nb)[0] for f in (0, 1)]
+        accs = {}
+        for impl, name in ((L.SPEC_IMPL_CUFFT, "cufft"), (L.SPEC_IMPL_SEPARABLE, "separable")):
+            a32 = L.Lattice(workload_config(L, L.FP32_KAHAN, impl=impl))
+            init_state(a32, 4242)
+            a32.symp(4, dt, steps_acc)
+            e32 = a32.energies()
+            acc = {"steps": steps_acc}
+            for f in (0, 1):
+                S32, _ = a32.spectrum(L.SPEC_FLD, f, L.SPEC_WEIGHTED, nb)
+                live = np.arange(nb) >= 1
+                rel = np.abs(S32[live] - S64[f][live]) / np.maximum(np.abs(S64[f][live]), 1e-300)
+                acc[f"pk_field{f}_max_rel_err"] = float(np.max(rel[: n // 4]))
+            acc["a_rel_err"] = abs(e32[L.E_A] - e64[L.E_A]) / e64[L.E_A]
+            acc["energy_rel_err"] = abs(e32[L.E_RHO] - e64[L.E_RHO]) / abs(e64[L.E_RHO])
+            acc["friedmann_residual_fp32"] = float(e32[L.E_RESIDUAL])
+            accs[name] = acc
+            a32.close()
+        accs["friedmann_residual_fp64"] = float(e64[L.E_RESIDUAL])
+        accs["friedmann_residual_initial"] = float(e0[L.E_RESIDUAL])
+        out["accuracy_vs_fp64_gpu"] = accs
         g64.close()
     # ---- end to end through the C ABI with pinned host arrays (Fortran layout)
     sub = args.e2e_sub
@@ -363,10 +401,14 @@ def diagnostics(L, g, args, dt, ms_step):
     el = time.perf_counter() - t0
     L.host_free(hf)
     L.host_free(hp)
-    out["e2e"] = {"value": N * sub * reps / el, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
-                  "d2h_bytes_per_step": 2 * nbytes + 8 * L.NENERGY,
-                  "step": f"lat_upload + lat_symp(4, dt, {sub}) + lat_energies + lat_download "
-                          "(FP64 Fortran-layout pinned host arrays)"}
+    out["e2e"] = {"value": N * sub * reps / el, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes / sub,
+                  "d2h_bytes_per_step": (2 * nbytes + 8 * L.NENERGY) / sub,
+                  "steps_per_call": sub, "calls": reps,
+                  "call": f"lat_upload + lat_symp(4, dt, {sub}) + lat_energies + lat_download "
+                          "(FP64 Fortran-layout pinned host arrays, host clock around the calls)"}
+    # ---- the other workloads of the engine (FD stencil paths)
+    if not args.no_fd:
+        out["fd_workloads"] = fd_workloads(L, hbm)
     # ---- CPU restatement on the host cores
     if not args.no_cpu:
         rate, cores, done, el = cpu_rate(steps_budget_s=args.cpu_budget, max_steps=args.cpu_steps)
@@ -375,6 +417,92 @@ def diagnostics(L, g, args, dt, ms_step):
                                          f"({el:.1f} s) after 1 warm-up step; CPU restatement of the "
                                          "Fortran reference, OpenMP"}
     return out
+
+
+def fd_workloads(L, hbm):
+    """Site-updates/s and HBM fraction of the FD kick+drift passes."""
+    res = {}
+    # plain method: one field, phi^4, 64^3, L = 20, 7-point, leapfrog, dt = dx/10, FP64
+    n = 64
+    c = L.make_config(n, nfld=1, length=20.0, laplacian=L.LAP_FD7, precision=L.FP64, model=L.MODEL_PHI4)
+    g = L.Lattice(c)
+    g.init_vacuum(1000, [1.0], [0.0], [3.0], amp=1e-8, kcut_frac=0.5)
+    dt = 20.0 / n / 10
+    g.symp(2, dt, 10)
+    g.sync()
+    g.mark(0)
+    g.symp(2, dt, 2000)
+    g.mark(1)
+    ms = g.mark_elapsed(0, 1)
+    res["phi4_64cube_fd7_fp64_leapfrog"] = {"steps": 2000, "ms_per_step": ms / 2000,
+                                            "value": n ** 3 * 2000 / (ms * 1e-3), "unit": UNIT,
+                                            "note": "whole 2000-step run, one symp2 call replayed as a CUDA graph"}
+    g.close()
+    # bubble collision with GW sourcing: 512^3, L = 128, 27-point, leapfrog, dt = dx/10, FP32 + Kahan
+    n = 512
+    g = L.Lattice(bubble_config(L, n))
+    init_bubbles(g, n)
+    dt = 0.25 / 10
+    g.symp(2, dt, 3)
+    g.sync()
+    K = 20
+    g.mark(0)
+    g.symp(2, dt, K)
+    g.mark(1)
+    ms = g.mark_elapsed(0, 1)
+    g.timing(True)
+    g.timing_reset()
+    g.symp(2, dt, 5)
+    g.sync()
+    tkd, nkd = g.timing_read(L.K_KICKDRIFT)
+    g.timing(False)
+    bytes_kd = 120 * n ** 3  # phi (Kahan) 24 B + 6 u_ij and 6 pi_ij read+write 96 B
+    ach = bytes_kd / (tkd / nkd * 1e-3) / 1e9 if nkd else None
+    res["bubbles_512cube_fd27_gw_fp32"] = {"steps": K, "ms_per_step": ms / K, "value": n ** 3 * K / (ms * 1e-3),
+                                           "unit": UNIT, "kickdrift_avg_us": 1e3 * tkd / max(nkd, 1),
+                                           "kickdrift_achieved_gbs": ach,
+                                           "kickdrift_frac": ach / hbm if ach else None,
+                                           "algorithmic_bytes_per_site": 120}
+    S, W = g.gw_spectrum(256)
+    res["bubbles_512cube_fd27_gw_fp32"]["gw_spectrum_bins_nonzero"] = int(np.count_nonzero(W))
+    g.close()
+    return res
+
+
+def bubble_config(L, n):
+    """Bubble collision with GW sourcing: L = n/4, 27-point, DEFROST split, FP32 + Kahan."""
+    return L.make_config(n, nfld=1, length=n / 4.0, laplacian=L.LAP_FD27, precision=L.FP32_KAHAN,
+                         split_order=L.SPLIT_DEFROST, model=L.MODEL_DOUBLE_WELL, model_params=(0.01,), gw=True,
+                         gw_coupling=2.0)
+
+
+def init_bubbles(g, n):
+    ln = n / 4.0
+    g.init_bubbles([[0.34375 * ln, 0.5 * ln, 0.5 * ln], [0.65625 * ln, 0.5 * ln, 0.5 * ln]], 0.09375 * ln,
+                   math.sqrt(2.0))
+
+
+def run_fd_case(L, args, local):
+    """The FD bubble workload alone at side --n (used for profiling captures)."""
+    n = args.n
+    c = bubble_config(L, n)
+    c.device = local
+    g = L.Lattice(c)
+    init_bubbles(g, n)
+    dt = 0.25 / 10
+    g.symp(2, dt, args.warmup)
+    g.sync()
+    l0 = g.launch_count()
+    g.mark(0)
+    g.symp(2, dt, args.steps)
+    g.mark(1)
+    ms = g.mark_elapsed(0, 1)
+    print(json.dumps({"metric": f"site-updates/s @{n}^3 FD27 bubbles + GW, leapfrog, FP32-Kahan",
+                      "value": n ** 3 * args.steps / (ms * 1e-3), "unit": UNIT, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                      "gpu_launches": g.launch_count() - l0}))
+    g.close()
+    return 0
 
 
 def main():
@@ -390,7 +518,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fd", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline number only")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--spectral-impl", default="auto", choices=["auto", "cufft", "separable"])
+    ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling cases; the metric is at 256)")
+    ap.add_argument("--case", default="headline", choices=["headline", "fd-bubbles"],
+                    help="fd-bubbles: the 27-point bubble-collision workload with GW sourcing at side --n")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

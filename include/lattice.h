@@ -90,8 +90,16 @@ typedef struct lat_config {
   double stencil[5];         /* (c0,c1,c2,c3,cc); all zero = default of the chosen stencil */
   double gw_coupling;        /* kappa in pi_ij' = lap u_ij + kappa d_i phi d_j phi */
   int32_t device;            /* CUDA ordinal                                */
-  int32_t reserved[7];
+  int32_t spectral_impl;     /* enum lat_spectral_impl                      */
+  int32_t reserved[6];
 } lat_config;
+
+/* How a spectral kick computes its Laplacian.  CUFFT: 3D R2C, -k^2/N multiply
+ * and C2R (any size).  SEPARABLE: three passes of in-register 1D transforms,
+ * one per axis (sides 16..512, powers of two), which also transform the FP32
+ * field with its Kahan compensation.  AUTO: cuFFT until lat_autotune times
+ * both on the handle's lattice and keeps the faster. */
+enum lat_spectral_impl { LAT_SPEC_IMPL_AUTO = 0, LAT_SPEC_IMPL_CUFFT = 1, LAT_SPEC_IMPL_SEPARABLE = 2 };
 
 typedef struct lat_s lat_t;
 
@@ -275,7 +283,10 @@ enum lat_kclass {
   LAT_K_FFT_C2R = 5,     /* cuFFT inverse */
   LAT_K_GW = 6,          /* GW kick+drift */
   LAT_K_OTHER = 7,
-  LAT_NKCLASS = 8
+  LAT_K_SEP_X = 8,       /* separable spectral pass X: drift + d2/dx2 */
+  LAT_K_SEP_Y = 9,       /* separable spectral pass Y: + d2/dy2 */
+  LAT_K_SEP_Z = 10,      /* separable spectral pass Z: + d2/dz2 and kick */
+  LAT_NKCLASS = 11
 };
 int lat_timing_enable(lat_t* h, int32_t on);
 /* total milliseconds and launch count of one class since the last reset */
@@ -301,8 +312,9 @@ int lat_host_free(void* ptr);
  * results are cached in `cache_path` (JSON lines) keyed by size, precision,
  * stencil and device, and reused when present.  cache_path may be NULL. */
 int lat_autotune(lat_t* h, const char* cache_path);
-/* The tile choice in use: tx, ty, zchunk, block threads, blocks per SM. */
-int lat_tuning_get(const lat_t* h, int32_t out[5]);
+/* The choice in use: FD tile tx, ty, zchunk; pointwise block threads, blocks
+ * per SM; spectral path (LAT_SPEC_IMPL_CUFFT or LAT_SPEC_IMPL_SEPARABLE). */
+int lat_tuning_get(const lat_t* h, int32_t out[6]);
 
 #ifdef __cplusplus
 }

@@ -41,10 +41,11 @@ SPLIT_PSEUDOSPEC, SPLIT_DEFROST = 0, 1
 MODEL_PHI4, MODEL_PHI4_G2, MODEL_DOUBLE_WELL, MODEL_FREE = 0, 1, 2, 3
 SPEC_FLD, SPEC_FLDP = 0, 1
 SPEC_WEIGHTED, SPEC_COUNT = 0, 1
+SPEC_IMPL_AUTO, SPEC_IMPL_CUFFT, SPEC_IMPL_SEPARABLE = 0, 1, 2
 E_KE, E_GE_LAP, E_GE_GRAD, E_PE, E_RHO, E_GRAV, E_RESIDUAL, E_A, E_AP, E_MEAN0, E_MEAN1, E_GW = range(12)
 NENERGY = 12
-K_KICKDRIFT, K_DRIFT, K_KICK, K_KMUL, K_FFT_R2C, K_FFT_C2R, K_GW, K_OTHER = range(8)
-NKCLASS = 8
+K_KICKDRIFT, K_DRIFT, K_KICK, K_KMUL, K_FFT_R2C, K_FFT_C2R, K_GW, K_OTHER, K_SEP_X, K_SEP_Y, K_SEP_Z = range(11)
+NKCLASS = 11
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_TIMEOUT", 4: "ERR_NAN", 5: "ERR_ALLOC",
           6: "ERR_STATE", 7: "ERR_IO", 8: "ERR_UNSUPPORTED"}
 
@@ -60,7 +61,8 @@ class LatConfig(C.Structure):
                 ("len", C.c_double), ("laplacian", C.c_int32), ("background", C.c_int32),
                 ("precision", C.c_int32), ("split_order", C.c_int32), ("model", C.c_int32),
                 ("gw", C.c_int32), ("model_params", C.c_double * 4), ("stencil", C.c_double * 5),
-                ("gw_coupling", C.c_double), ("device", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("gw_coupling", C.c_double), ("device", C.c_int32), ("spectral_impl", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 _lib = None
@@ -136,7 +138,7 @@ def _dp(a: np.ndarray | None):
 
 def make_config(n, nfld=1, length=1.0, laplacian=LAP_SPECTRAL, background=BG_MINKOWSKI, precision=FP64,
                 split_order=SPLIT_PSEUDOSPEC, model=MODEL_PHI4, model_params=(1.0,), stencil=None,
-                gw=False, gw_coupling=0.0, device=0) -> LatConfig:
+                gw=False, gw_coupling=0.0, device=0, spectral_impl=SPEC_IMPL_AUTO) -> LatConfig:
     nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
     c = LatConfig()
     c.nx, c.ny, c.nz, c.nfld, c.len = nx, ny, nz, nfld, float(length)
@@ -149,6 +151,7 @@ def make_config(n, nfld=1, length=1.0, laplacian=LAP_SPECTRAL, background=BG_MIN
             c.stencil[i] = float(v)
     c.gw_coupling = float(gw_coupling)
     c.device = device
+    c.spectral_impl = spectral_impl
     return c
 
 
@@ -357,7 +360,7 @@ class Lattice:
         _check(_lib.lat_autotune(self._h, None if cache_path is None else str(cache_path).encode()))
 
     def tuning(self) -> list[int]:
-        out = (C.c_int32 * 5)()
+        out = (C.c_int32 * 6)()
         _check(_lib.lat_tuning_get(self._h, out))
         return list(out)
 

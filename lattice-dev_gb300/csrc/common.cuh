@@ -30,6 +30,8 @@ struct DevScalars {
   double ge2;      // (1/N) sum_k k^2 |F_k|^2 over fields = -sum_x phi lap phi (last k-space pass)
   double ke2;      // sum_x pi^2 of the last drift pass (diagnostic)
   double red[16];  // raw sums of the last stand-alone reduction (energies)
+  double gsum[3];  // -sum phi d2_axis(phi) of the separable passes X, Y, Z
+  double mean[4];  // lattice means of the fields (spectral shift of the separable passes)
   unsigned int err;  // bit 0: NaN/Inf met in a reduction
   unsigned int pad[3];
 };

@@ -69,6 +69,8 @@ struct GraphEntry {
   int nsteps;
   int cur, ucur;
   int cur_after, ucur_after;
+  void *fldc, *fldp;              // current compensation / momentum buffers at capture
+  void *fldc_after, *fldp_after;  // and after the captured call
   int64_t kernels;
   cudaGraphExec_t exec;
 };
@@ -88,9 +90,12 @@ struct lat_s {
 
   void* fld[2] = {nullptr, nullptr};
   int cur = 0;
-  void* fldc = nullptr;
-  void* fldp = nullptr;
+  void* fldc = nullptr;      // current Kahan compensation buffer
+  void* fldp = nullptr;      // current momentum buffer
   void* lap = nullptr;
+  void* fldc_alt = nullptr;  // second buffers the separable passes write to
+  void* fldp_alt = nullptr;
+  void* lap_alt = nullptr;
   void* Fk = nullptr;  // max(nf,2) * M complex
   void* u[2] = {nullptr, nullptr};
   int ucur = 0;
@@ -113,6 +118,14 @@ struct lat_s {
   size_t fft_work_size = 0;
 
   double tglobal[3] = {0, 0, 0};
+
+  cufftHandle p_d2z1 = 0;          // FP64 transform for spectra of FP32 fields
+  bool have_d2z1 = false;
+  void* Fk64 = nullptr;            // 2 * M double2
+
+  bool sep_ok = false;            // separable spectral passes available for these sizes
+  bool sep = false;               // and in use
+  void* tw[3] = {nullptr, nullptr, nullptr};  // W_N^j per axis, field precision
 
   int fd_ty = 8, fd_zc = 32;
   int pw_grid = 0, pw_block = 256;
@@ -174,6 +187,10 @@ struct Timed {
 };
 
 // ------------------------------------------------------------- helpers
+bool getenv_flag(const char* name) {
+  const char* v = getenv(name);
+  return v && v[0] == '1';
+}
 bool conformal(const lat_s* h) { return h->cfg.background == LAT_BG_CONFORMAL; }
 bool spectral(const lat_s* h) { return h->cfg.laplacian == LAT_LAP_SPECTRAL; }
 int n_terms(const lat_s* h) {
@@ -369,11 +386,104 @@ int exec_plain(lat_s* h, const std::vector<Op>& ops) {
   return LAT_OK;
 }
 
+// One separable spectral pass (k_sep.cuh) along `axis`.
+int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
+  static const int kcls[3] = {LAT_K_SEP_X, LAT_K_SEP_Y, LAT_K_SEP_Z};
+  Timed t(h, kcls[axis]);
+  SepArgs a{};
+  a.nx = h->nx; a.ny = h->ny; a.nz = h->nz; a.nf = h->nf;
+  a.phi = h->fld[h->cur];
+  a.phic = h->fldc;
+  a.pi = h->fldp;
+  a.lap = axis == 2 ? h->lap_alt : h->lap;
+  a.phi_out = h->fld[1 - h->cur];
+  a.phic_out = h->fldc_alt;
+  a.pi_out = h->fldp_alt;
+  a.lap_out = axis == 0 ? h->lap : h->lap_alt;
+  a.twN = h->tw[axis];
+  const int n = axis == 0 ? h->nx : (axis == 1 ? h->ny : h->nz);
+  const double dk = axis == 0 ? h->dkx : (axis == 1 ? h->dky : h->dkz);
+  a.dk2 = dk * dk;
+  a.model = model_of(h);
+  a.hk = hk; a.hg = hg; a.hd = hd;
+  a.Nd = (double)h->N;
+  a.conf = conformal(h) ? 1 : 0;
+  const int64_t pairs = h->nf == 2 ? 1 : 2;
+  a.nlines = axis == 0 ? (int64_t)h->ny * h->nz / pairs
+                       : (axis == 1 ? (int64_t)h->nx * h->nz / pairs : (int64_t)h->nx * h->ny / pairs);
+  a.sc = h->sc;
+  a.rb = red(h);
+  int st;
+  switch (n) {
+    case 16: st = launch_sep_16(a, h->prec, axis, h->stream); break;
+    case 32: st = launch_sep_32(a, h->prec, axis, h->stream); break;
+    case 64: st = launch_sep_64(a, h->prec, axis, h->stream); break;
+    case 128: st = launch_sep_128(a, h->prec, axis, h->stream); break;
+    case 256: st = launch_sep_256(a, h->prec, axis, h->stream); break;
+    case 512: st = launch_sep_512(a, h->prec, axis, h->stream); break;
+    default: return set_error(LAT_ERR_UNSUPPORTED, "separable pass length");
+  }
+  if (st != LAT_OK) return st;
+  if (axis == 0) {  // drifted fields now live in the second buffers
+    h->cur = 1 - h->cur;
+    std::swap(h->fldc, h->fldc_alt);
+  } else if (axis == 2) {  // kicked momenta
+    std::swap(h->fldp, h->fldp_alt);
+  }
+  return LAT_OK;
+}
+
+// Separable spectral execution of an op list: every kick becomes the passes
+// X (carrying the preceding drift), Y and Z (the kick); the last drift runs
+// stand-alone.  Returns LAT_ERR_UNSUPPORTED (nothing launched) when the list
+// is not D (G K G D | K D+)* shaped.
+int exec_sep(lat_s* h, const std::vector<Op>& ops) {
+  const bool conf = conformal(h);
+  struct Grp { double hk, hg, hd; };
+  std::vector<Grp> grp;
+  double lead = 0;
+  size_t i = 0;
+  while (i < ops.size() && ops[i].t == 'D') {
+    lead += ops[i++].h;
+    if (conf) break;
+  }
+  while (i < ops.size()) {
+    if (conf) {
+      if (i + 3 < ops.size() && ops[i].t == 'G' && ops[i + 1].t == 'K' && ops[i + 2].t == 'G' && ops[i + 3].t == 'D' &&
+          ops[i].h == ops[i + 2].h) {
+        grp.push_back({ops[i + 1].h, ops[i].h, ops[i + 3].h});
+        i += 4;
+        continue;
+      }
+    } else if (ops[i].t == 'K' && i + 1 < ops.size() && ops[i + 1].t == 'D') {
+      Grp g{ops[i].h, 0.0, 0.0};
+      ++i;
+      while (i < ops.size() && ops[i].t == 'D') g.hd += ops[i++].h;
+      grp.push_back(g);
+      continue;
+    }
+    return LAT_ERR_UNSUPPORTED;
+  }
+  double pending = lead;
+  for (const Grp& g : grp) {
+    RET(sep_pass(h, 0, 0.0, 0.0, pending));
+    RET(sep_pass(h, 1, 0.0, 0.0, 0.0));
+    RET(sep_pass(h, 2, g.hk, g.hg, 0.0));
+    pending = g.hd;
+  }
+  if (pending != 0.0) RET(exec_drift(h, pending));
+  return LAT_OK;
+}
+
 int exec_fused(lat_s* h, const std::vector<Op>& in) {
   std::vector<Op> ops;
   for (const Op& o : in)
     if (o.t != 'M') ops.push_back(o);
   const bool conf = conformal(h);
+  if (h->sep && (!conf || h->cfg.split_order == LAT_SPLIT_PSEUDOSPEC)) {
+    const int st = exec_sep(h, ops);
+    if (st != LAT_ERR_UNSUPPORTED) return st;
+  }
   if (conf && !spectral(h)) return exec_plain(h, ops);
   if (conf && h->cfg.split_order == LAT_SPLIT_DEFROST) return exec_plain(h, ops);
   size_t i = 0;
@@ -512,7 +622,7 @@ int src_ptr(lat_s* h, int what, int field, const void** p) {
   return LAT_OK;
 }
 
-int run_spectrum(lat_s* h, const void* F1, const void* F2, int mode, int nbins, double* hostout) {
+int run_spectrum(lat_s* h, const void* F1, const void* F2, int mode, int nbins, double* hostout, int prec) {
   SpecArgs s{};
   s.nx = h->nx; s.ny = h->ny; s.nz = h->nz;
   s.F1 = F1; s.F2 = F2; s.mode = mode; s.nbins = nbins;
@@ -523,7 +633,7 @@ int run_spectrum(lat_s* h, const void* F1, const void* F2, int mode, int nbins, 
   s.block = 256;
   {
     Timed t(h, LAT_K_OTHER);
-    RET(launch_spectrum(s, h->prec, h->stream));
+    RET(launch_spectrum(s, prec, h->stream));
   }
   CK(cudaMemcpyAsync(hostout, h->spec_out, sizeof(double) * 3 * nbins, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -531,6 +641,43 @@ int run_spectrum(lat_s* h, const void* F1, const void* F2, int mode, int nbins, 
 }
 
 const int kMaxBins = 2048;
+
+// Half spectrum of one field or momentum array for the output routines.  An
+// FP32 field is transformed in FP64 from phi_hi - c, so a field sitting near
+// a large mean keeps the digits of its fluctuation (an FP32 transform of
+// phi_hi alone would not).  Returns the precision of the spectrum written.
+int output_spectrum(lat_s* h, int what, int field, int slot, void** Fout, int* prec) {
+  const void* src;
+  RET(src_ptr(h, what, field, &src));
+  if (h->prec == LAT_FP64) {
+    void* F = (char*)h->Fk + (size_t)slot * h->M * h->csz;
+    RET(fft_exec_r2c(h, h->p_r2c1, src, F));
+    *Fout = F;
+    *prec = LAT_FP64;
+    return LAT_OK;
+  }
+  if (!h->Fk64) CK(cudaMalloc(&h->Fk64, (size_t)2 * h->M * sizeof(double2)));
+  if (!h->have_d2z1) {
+    CF(cufftCreate(&h->p_d2z1));
+    int n[3] = {h->nz, h->ny, h->nx};
+    size_t ws = 0;
+    CF(cufftMakePlanMany(h->p_d2z1, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1, &ws));
+    CF(cufftSetStream(h->p_d2z1, h->stream));
+    h->have_d2z1 = true;
+  }
+  RET(ensure_stage(h, (size_t)std::max(h->nf, 2) * h->N));
+  const void* comp = (what == LAT_SPEC_FLD && h->fldc) ? (const char*)h->fldc + (size_t)field * h->N * h->rsz : nullptr;
+  double* tmp = h->stage + (size_t)slot * h->N;
+  RET(launch_to_fp64(src, comp, h->N, h->prec, tmp, h->stream));
+  void* F = (double2*)h->Fk64 + (size_t)slot * h->M;
+  {
+    Timed t(h, LAT_K_FFT_R2C);
+    CF(cufftExecD2Z(h->p_d2z1, tmp, (cufftDoubleComplex*)F));
+  }
+  *Fout = F;
+  *prec = LAT_FP64;
+  return LAT_OK;
+}
 
 }  // namespace
 
@@ -545,7 +692,12 @@ int lat_destroy(lat_t* h) {
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_graphs(h);
-  void* bufs[] = {h->fld[0], h->fld[1], h->fldc, h->fldp, h->lap, h->Fk, h->u[0], h->u[1], h->pu, h->Fk6,
+  for (void* t : h->tw)
+    if (t) cudaFree(t);
+  if (h->Fk64) cudaFree(h->Fk64);
+  if (h->have_d2z1) cufftDestroy(h->p_d2z1);
+  void* bufs[] = {h->fld[0], h->fld[1], h->fldc, h->fldp, h->lap, h->fldc_alt, h->fldp_alt, h->lap_alt, h->Fk,
+                  h->u[0], h->u[1], h->pu, h->Fk6,
                   h->sc, h->rb.partials, h->rb.counter, h->spec_part, h->spec_out, h->spec_counter, h->stage,
                   h->fft_work};
   for (void* b : bufs)
@@ -661,14 +813,58 @@ int lat_create(lat_t** out, const lat_config* cfg) {
     if ((st = make_plan(h, &h->p_r2c, &h->have_r2c, true, h->nf))) return bail(st);
     if ((st = make_plan(h, &h->p_c2r, &h->have_c2r, false, h->nf))) return bail(st);
   }
+  if (spectral(h)) {
+    auto pow2ok = [](int n) { return n >= 16 && n <= 512 && (n & (n - 1)) == 0; };
+    auto cols = [&](int n) {  // x-columns per block of a y or z pass of length n
+      switch (n) {
+        case 16: return sep_columns_16(h->prec, h->nf);
+        case 32: return sep_columns_32(h->prec, h->nf);
+        case 64: return sep_columns_64(h->prec, h->nf);
+        case 128: return sep_columns_128(h->prec, h->nf);
+        case 256: return sep_columns_256(h->prec, h->nf);
+        default: return sep_columns_512(h->prec, h->nf);
+      }
+    };
+    h->sep_ok = pow2ok(h->nx) && pow2ok(h->ny) && pow2ok(h->nz);
+    // the passes need whole column blocks and (one field) an even number of x-rows
+    if (h->sep_ok) h->sep_ok = h->nx % cols(h->ny) == 0 && h->nx % cols(h->nz) == 0;
+    if (cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !h->sep_ok)
+      return bail(set_error(LAT_ERR_UNSUPPORTED, "separable spectral passes need power-of-two sides 16..512"));
+    h->sep = h->sep_ok && cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !getenv_flag("LAT_NO_SEPARABLE");
+    if (h->sep_ok) {
+      if ((st = alloc(&h->fld[1], fb))) return bail(st);
+      if (h->prec == LAT_FP32_KAHAN && (st = alloc(&h->fldc_alt, fb))) return bail(st);
+      if ((st = alloc(&h->fldp_alt, fb))) return bail(st);
+      if ((st = alloc(&h->lap_alt, fb))) return bail(st);
+    }
+    if (h->sep) {
+      const int dims[3] = {h->nx, h->ny, h->nz};
+      for (int ax = 0; ax < 3; ++ax) {
+        const int n = dims[ax];
+        std::vector<double> w64(2 * n);
+        std::vector<float> w32(2 * n);
+        for (int j = 0; j < n; ++j) {
+          const long double ang = -6.283185307179586476925286766559L * (long double)j / (long double)n;
+          w64[2 * j] = (double)cosl(ang);
+          w64[2 * j + 1] = (double)sinl(ang);
+          w32[2 * j] = (float)w64[2 * j];
+          w32[2 * j + 1] = (float)w64[2 * j + 1];
+        }
+        if ((st = alloc(&h->tw[ax], (size_t)n * h->csz))) return bail(st);
+        const void* src = h->prec == LAT_FP64 ? (const void*)w64.data() : (const void*)w32.data();
+        if ((e = cudaMemcpyAsync(h->tw[ax], src, (size_t)n * h->csz, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+          return bail(cuda_fail(e, "twiddle upload"));
+        if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "twiddle upload"));
+      }
+    }
+  }
   h->ev_pool.resize(4096);
   for (auto& ev : h->ev_pool) {
     cudaEventCreate(&ev.a);
     cudaEventCreate(&ev.b);
   }
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "create sync"));
-  const char* ng = getenv("LAT_NO_GRAPHS");
-  h->use_graphs = !(ng && ng[0] == '1');
+  h->use_graphs = !getenv_flag("LAT_NO_GRAPHS");
   *out = h;
   return LAT_OK;
 }
@@ -791,17 +987,23 @@ int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps) {
     return LAT_OK;
   }
   for (auto& ge : h->graphs) {
-    if (ge.order == order && ge.dt == dt && ge.nsteps == nsteps && ge.cur == h->cur && ge.ucur == h->ucur) {
+    if (ge.order == order && ge.dt == dt && ge.nsteps == nsteps && ge.cur == h->cur && ge.ucur == h->ucur &&
+        ge.fldc == h->fldc && ge.fldp == h->fldp) {
       CK(cudaGraphLaunch(ge.exec, h->stream));
       h->launches += ge.kernels;
       h->cur = ge.cur_after;
       h->ucur = ge.ucur_after;
+      if (h->fldc != ge.fldc_after) std::swap(h->fldc, h->fldc_alt);
+      if (h->fldp != ge.fldp_after) std::swap(h->fldp, h->fldp_alt);
       std::memcpy(h->tglobal, tg, sizeof(tg));
       return LAT_OK;
     }
   }
   GraphEntry ge{};
   ge.order = order; ge.dt = dt; ge.nsteps = nsteps; ge.cur = h->cur; ge.ucur = h->ucur;
+  ge.fldc = h->fldc; ge.fldp = h->fldp;
+  void* const c_alt0 = h->fldc_alt;
+  void* const p_alt0 = h->fldp_alt;
   const int64_t before = h->launches;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
   int st = exec_fused(h, ops);
@@ -810,12 +1012,16 @@ int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps) {
   if (st != LAT_OK) {
     if (graph) cudaGraphDestroy(graph);
     h->cur = ge.cur; h->ucur = ge.ucur;
+    h->fldc = ge.fldc; h->fldc_alt = c_alt0;
+    h->fldp = ge.fldp; h->fldp_alt = p_alt0;
     return st;
   }
   if (e != cudaSuccess) return cuda_fail(e, "graph capture");
   ge.kernels = h->launches - before;
   ge.cur_after = h->cur;
   ge.ucur_after = h->ucur;
+  ge.fldc_after = h->fldc;
+  ge.fldp_after = h->fldp;
   e = cudaGraphInstantiate(&ge.exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
@@ -896,11 +1102,11 @@ int lat_spectrum(lat_t* h, int32_t what, int32_t field, int32_t mode, int32_t nb
   if (nbins < 1 || nbins > kMaxBins) return set_error(LAT_ERR_ARG, "nbins out of range");
   if (mode != LAT_SPEC_WEIGHTED && mode != LAT_SPEC_COUNT) return set_error(LAT_ERR_ARG, "bad spectrum mode");
   ApiGuard g(h);
-  const void* src;
-  RET(src_ptr(h, what, field, &src));
-  RET(fft_exec_r2c(h, h->p_r2c1, src, h->Fk));
+  void* F;
+  int sp;
+  RET(output_spectrum(h, what, field, 0, &F, &sp));
   std::vector<double> o(3 * nbins);
-  RET(run_spectrum(h, h->Fk, nullptr, mode, nbins, o.data()));
+  RET(run_spectrum(h, F, nullptr, mode, nbins, o.data(), sp));
   for (int l = 0; l < nbins; ++l) {
     W[l] = o[nbins + l];
     S[l] = W[l] != 0.0 ? o[l] / W[l] : o[l];
@@ -913,14 +1119,12 @@ int lat_crossspec(lat_t* h, int32_t what1, int32_t field1, int32_t what2, int32_
   if (!h || !S_re || !S_im) return set_error(LAT_ERR_ARG, "null argument");
   if (nbins < 1 || nbins > kMaxBins) return set_error(LAT_ERR_ARG, "nbins out of range");
   ApiGuard g(h);
-  const void *s1, *s2;
-  RET(src_ptr(h, what1, field1, &s1));
-  RET(src_ptr(h, what2, field2, &s2));
-  char* F2 = (char*)h->Fk + (size_t)h->M * h->csz;
-  RET(fft_exec_r2c(h, h->p_r2c1, s1, h->Fk));
-  RET(fft_exec_r2c(h, h->p_r2c1, s2, F2));
+  void *F1, *F2;
+  int sp;
+  RET(output_spectrum(h, what1, field1, 0, &F1, &sp));
+  RET(output_spectrum(h, what2, field2, 1, &F2, &sp));
   std::vector<double> o(3 * nbins);
-  RET(run_spectrum(h, h->Fk, F2, 2, nbins, o.data()));
+  RET(run_spectrum(h, F1, F2, 2, nbins, o.data(), sp));
   for (int l = 0; l < nbins; ++l) {
     const double w = o[nbins + l];
     S_re[l] = w != 0.0 ? o[l] / w : o[l];
@@ -1235,8 +1439,9 @@ std::string tune_key(lat_s* h) {
   cudaDeviceProp prop{};
   cudaGetDeviceProperties(&prop, h->dev);
   char buf[256];
-  snprintf(buf, sizeof(buf), "%s|sm%d%d|p%d|lap%d|bg%d|nf%d|gw%d|%dx%dx%d", prop.name, prop.major, prop.minor,
-           h->prec, h->cfg.laplacian, h->cfg.background, h->nf, h->cfg.gw, h->nx, h->ny, h->nz);
+  snprintf(buf, sizeof(buf), "%s|sm%d%d|p%d|lap%d|bg%d|nf%d|gw%d|%dx%dx%d|impl%d", prop.name, prop.major, prop.minor,
+           h->prec, h->cfg.laplacian, h->cfg.background, h->nf, h->cfg.gw, h->nx, h->ny, h->nz,
+           h->cfg.spectral_impl);
   return buf;
 }
 
@@ -1249,10 +1454,11 @@ bool tune_lookup(const char* path, const std::string& key, int v[4]) {
   const std::string pat = "\"key\": \"" + key + "\"";
   while (fgets(line, sizeof(line), fp)) {
     if (!strstr(line, pat.c_str())) continue;
-    int a, b, c, d;
+    int a, b, c, d, e = 0;
     const char* q = strstr(line, "\"ty\":");
-    if (q && sscanf(q, "\"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d", &a, &b, &c, &d) == 4) {
-      v[0] = a; v[1] = b; v[2] = c; v[3] = d;
+    if (q && sscanf(q, "\"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d, \"sep\": %d", &a, &b, &c, &d,
+                    &e) >= 4) {
+      v[0] = a; v[1] = b; v[2] = c; v[3] = d; v[4] = e;
       found = true;
     }
   }
@@ -1290,9 +1496,10 @@ int lat_autotune(lat_t* h, const char* cache_path) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   const std::string key = tune_key(h);
-  int v[4];
+  int v[5] = {0, 0, 0, 0, 0};
   if (tune_lookup(cache_path, key, v)) {
     h->fd_ty = v[0]; h->fd_zc = std::min(v[1], h->nz); h->pw_block = v[2]; h->pw_grid = h->nsm * v[3];
+    if (h->sep_ok && h->cfg.spectral_impl == LAT_SPEC_IMPL_AUTO) h->sep = v[4] != 0;
     free_graphs(h);
     return LAT_OK;
   }
@@ -1308,6 +1515,10 @@ int lat_autotune(lat_t* h, const char* cache_path) {
     return LAT_OK;
   };
   const int cur0 = h->cur, ucur0 = h->ucur;
+  void* const c0 = h->fldc;
+  void* const c0a = h->fldc_alt;
+  void* const p0 = h->fldp;
+  void* const p0a = h->fldp_alt;
   RET(save(h->fld[h->cur], fb));
   RET(save(h->fldc, fb));
   RET(save(h->fldp, fb));
@@ -1361,10 +1572,35 @@ int lat_autotune(lat_t* h, const char* cache_path) {
     }
   h->pw_block = bpb;
   h->pw_grid = h->nsm * bbps;
+  // spectral Laplacian: cuFFT path against the separable passes, one substep each
+  if (st == LAT_OK && h->sep_ok && h->cfg.spectral_impl == LAT_SPEC_IMPL_AUTO) {
+    std::vector<Op> ops;
+    double tg[3] = {0, 0, 0};
+    Emitter em = emitter(h, &ops, tg);
+    st = em.symp(2, 1e-3, 2);
+    float tms[2] = {0, 0};
+    for (int impl = 0; impl < 2 && st == LAT_OK; ++impl) {
+      h->sep = impl == 1;
+      cudaEvent_t a, b;
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      st = exec_fused(h, ops);  // warm-up
+      cudaEventRecord(a, h->stream);
+      for (int r = 0; r < reps && st == LAT_OK; ++r) st = exec_fused(h, ops);
+      cudaEventRecord(b, h->stream);
+      cudaEventSynchronize(b);
+      cudaEventElapsedTime(&tms[impl], a, b);
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+    h->sep = tms[1] < tms[0];
+  }
   h->timing = was_timing;
   // restore
   h->cur = cur0;
   h->ucur = ucur0;
+  h->fldc = c0; h->fldc_alt = c0a;
+  h->fldp = p0; h->fldp_alt = p0a;
   void* dst[6] = {h->fld[h->cur], h->fldc, h->fldp, h->cfg.gw ? h->u[h->ucur] : nullptr,
                   h->cfg.gw ? h->pu : nullptr, h->sc};
   size_t sz[6] = {fb, fb, fb, gb, gb, sizeof(DevScalars)};
@@ -1378,17 +1614,18 @@ int lat_autotune(lat_t* h, const char* cache_path) {
   if (cache_path) {
     FILE* fp = fopen(cache_path, "a");
     if (fp) {
-      fprintf(fp, "{\"key\": \"%s\", \"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d}\n", key.c_str(),
-              h->fd_ty, h->fd_zc, h->pw_block, h->pw_grid / h->nsm);
+      fprintf(fp, "{\"key\": \"%s\", \"ty\": %d, \"zc\": %d, \"pw_block\": %d, \"pw_bps\": %d, \"sep\": %d}\n",
+              key.c_str(), h->fd_ty, h->fd_zc, h->pw_block, h->pw_grid / h->nsm, h->sep ? 1 : 0);
       fclose(fp);
     }
   }
   return LAT_OK;
 }
 
-int lat_tuning_get(const lat_t* h, int32_t out[5]) {
+int lat_tuning_get(const lat_t* h, int32_t out[6]) {
   if (!h || !out) return set_error(LAT_ERR_ARG, "null argument");
   out[0] = 32; out[1] = h->fd_ty; out[2] = h->fd_zc; out[3] = h->pw_block; out[4] = h->pw_grid / h->nsm;
+  out[5] = h->sep ? LAT_SPEC_IMPL_SEPARABLE : LAT_SPEC_IMPL_CUFFT;
   return LAT_OK;
 }
 

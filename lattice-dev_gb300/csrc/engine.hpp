@@ -65,6 +65,40 @@ struct PwArgs {
 };
 int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s);
 
+// Separable spectral passes (k_sep.cuh): one launch per axis per kick.
+struct SepArgs {
+  int nx, ny, nz, nf;
+  const void* phi;   // inputs
+  const void* phic;
+  const void* pi;
+  const void* lap;
+  void* phi_out;     // outputs: every updated array goes to its second buffer
+  void* phic_out;
+  void* pi_out;
+  void* lap_out;
+  const void* twN;  // W_N^j, j < N, of this axis, in the field precision
+  double dk2;       // (2 pi / (n dx))^2 of this axis
+  ModelP model;
+  double hk, hg, hd;
+  double Nd;
+  int conf;
+  int64_t nlines;   // complex lines of this pass
+  DevScalars* sc;
+  RedBuf rb;
+};
+int launch_sep_16(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int launch_sep_32(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int launch_sep_64(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int launch_sep_128(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int launch_sep_256(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int launch_sep_512(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int sep_columns_16(int precision, int nf);
+int sep_columns_32(int precision, int nf);
+int sep_columns_64(int precision, int nf);
+int sep_columns_128(int precision, int nf);
+int sep_columns_256(int precision, int nf);
+int sep_columns_512(int precision, int nf);
+
 // k-space multiply F *= -k^2/N with the Parseval sum of k^2|F|^2 (Hermitian
 // weights) into sc->ge2 when store_ge2 is set.
 struct KmulArgs {

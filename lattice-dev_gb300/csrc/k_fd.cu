@@ -25,6 +25,18 @@ __device__ __forceinline__ int pmod(int i, int n) {
   return r < 0 ? r + n : r;
 }
 
+__device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem, int bytes) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int G> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(G) : "memory");
+}
+
+constexpr int kFdMaxSlots = 4;  // halo'd plane elements one thread stages per plane (covers ty >= 2)
+
 template <typename R, bool KAHAN, int NF, bool GW, bool SEVEN, int MODE>
 __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   constexpr int NC = NF + (GW ? 6 : 0);
@@ -32,10 +44,11 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   const int TY = blockDim.y;
   const int Wd = TX + 2, PL = Wd * (TY + 2);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R* sm = reinterpret_cast<R*>(smem_raw);  // [2][NC][PL]
+  R* sm = reinterpret_cast<R*>(smem_raw);  // [3][NC][PL]: ring of planes z-1, z, z+1 (and the one in flight)
 
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int64_t N = (int64_t)nx * ny * nz;
+  const int64_t plane = (int64_t)nx * ny;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = tx + TX * ty, nthr = TX * TY;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
@@ -47,18 +60,36 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   const R* phi = static_cast<const R*>(a.phi_in);
   const R* uin = static_cast<const R*>(a.u_in);
 
-  auto load_plane = [&](int z, int b) {
-    const int zz = pmod(z, nz);
-    for (int i = tid; i < PL; i += nthr) {
+  // in-plane offsets (periodic wrap) of the tile elements this thread stages;
+  // the same for every plane, so the wrap arithmetic runs once per block
+  int slot_off[kFdMaxSlots];
+  int nslot = 0;
+#pragma unroll
+  for (int k = 0; k < kFdMaxSlots; ++k) {
+    const int i = tid + k * nthr;
+    slot_off[k] = 0;
+    if (i < PL) {
       const int r = i / Wd, cc = i - r * Wd;
       const int gx = pmod(x0 + cc - 1, nx), gy = pmod(y0 + r - 1, ny);
-      const int64_t off = ((int64_t)zz * ny + gy) * nx + gx;
+      slot_off[k] = gy * nx + gx;
+      nslot = k + 1;
+    }
+  }
+  // issue the asynchronous copy of plane z into ring buffer b
+  auto load_plane = [&](int z, int b) {
+    const int64_t zo = (int64_t)pmod(z, nz) * plane;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const R* src = c < NF ? phi + (int64_t)c * N : uin + (int64_t)(c - NF) * N;
-        sm[(b * NC + c) * PL + i] = src[off];
+    for (int k = 0; k < kFdMaxSlots; ++k) {
+      if (k < nslot) {
+        const int i = tid + k * nthr;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const R* src = c < NF ? phi + (int64_t)c * N : uin + (int64_t)(c - NF) * N;
+          cp_async_elem(sm + (b * NC + c) * PL + i, src + zo + slot_off[k], (int)sizeof(R));
+        }
       }
     }
+    cp_async_commit();
   };
 
   R wc[NC][3], ws1[NC][3], ws2[NC][3];
@@ -97,10 +128,15 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   using Acc = typename AccOf<R>::type;
   Acc acc_ge, acc_pe;
 
+  // ring: plane p (counted from z0-1) lives in buffer p % 3; two planes are in
+  // flight ahead of the one being filled
   load_plane(z0 - 1, 0);
+  load_plane(z0, 1);
+  load_plane(z0 + 1, 2);
+  cp_async_wait<2>();
   __syncthreads();
   fill(0, 0);
-  load_plane(z0, 1);
+  cp_async_wait<1>();
   __syncthreads();
   fill(1, 1);
 
@@ -111,12 +147,29 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   R* uo = static_cast<R*>(a.u_out);
 
   for (int z = z0; z < z1; ++z) {
-    const int bnext = (z - z0) & 1;  // buffer of plane z+1
-    load_plane(z + 1, bnext);
+    const int bnext = (z - z0 + 2) % 3;  // buffer of plane z+1
+    const int64_t s = ((int64_t)z * ny + y) * nx + x;
+    // this site's pointwise state, requested before the wait so that it lands
+    // while the plane ring catches up
+    R piv[NF], cpv[NF], puv[GW ? 6 : 1];
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NF; ++l) {
+        piv[l] = pi[(int64_t)l * N + s];
+        cpv[l] = (KAHAN && MODE == 0) ? phic[(int64_t)l * N + s] : R(0);
+      }
+      if (GW) {
+#pragma unroll
+        for (int g = 0; g < 6; ++g) puv[g] = pu[(int64_t)g * N + s];
+      }
+    }
+    // plane z+2 goes into the buffer of plane z-1, read two iterations ago
+    if (z + 1 < z1) load_plane(z + 2, (z - z0 + 3) % 3);
+    else cp_async_commit();  // keep one group per iteration
+    cp_async_wait<1>();
     __syncthreads();
     fill(bnext, 2);
     if (active) {
-      const int64_t s = ((int64_t)z * ny + y) * nx + x;
       R lap[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
@@ -136,11 +189,11 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
 #pragma unroll
       for (int l = 0; l < NF; ++l) {
         const int64_t sl = (int64_t)l * N + s;
-        const R pn = pi[sl] + (ck * lap[l] - cv * dv[l]);
+        const R pn = piv[l] + (ck * lap[l] - cv * dv[l]);
         pi[sl] = pn;
         if (MODE == 0) {
           if constexpr (KAHAN) {
-            R xv = f[l], cc = phic[sl];
+            R xv = f[l], cc = cpv[l];
             kahan_add(xv, cc, cd * pn);
             phio[sl] = xv;
             phic[sl] = cc;
@@ -169,7 +222,7 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
             src += di * dj;
           }
           const int64_t sg = (int64_t)g * N + s;
-          const R pn = pu[sg] + ck * (lap[NF + g] + kap * src);
+          const R pn = puv[g] + ck * (lap[NF + g] + kap * src);
           pu[sg] = pn;
           if (MODE == 0) uo[sg] = wc[NF + g][1] + cd * pn;
         }
@@ -206,7 +259,8 @@ int go(const FdArgs& a, cudaStream_t s, int* nb) {
   constexpr int NC = NF + (GW ? 6 : 0);
   dim3 block(32, a.ty);
   dim3 grid((a.nx + 31) / 32, (a.ny + a.ty - 1) / a.ty, (a.nz + a.zc - 1) / a.zc);
-  size_t smem = (size_t)2 * NC * 34 * (a.ty + 2) * sizeof(R);
+  size_t smem = (size_t)3 * NC * 34 * (a.ty + 2) * sizeof(R);
+  if (34 * (a.ty + 2) > kFdMaxSlots * 32 * a.ty) return set_error(LAT_ERR_ARG, "FD tile too narrow");
   auto k = fd_kernel<R, KAHAN, NF, GW, SEVEN, MODE>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

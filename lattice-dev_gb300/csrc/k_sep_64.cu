@@ -1,0 +1,9 @@
+// k_sep_64.cu -- separable spectral passes for lines of 64 points.
+#include "k_sep.cuh"
+
+namespace lat {
+int launch_sep_64(const SepArgs& a, int precision, int axis, cudaStream_t s) {
+  return sep::sep_dispatch<64>(a, precision, axis, s);
+}
+int sep_columns_64(int precision, int nf) { return sep::sep_columns<64>(precision, nf); }
+}  // namespace lat

@@ -1,0 +1,133 @@
+"""Cross-checks between the engine's execution paths on the GPU.
+
+* separable spectral passes (power-of-two sizes) vs the cuFFT 3D path
+  (forced with LAT_NO_SEPARABLE=1) on identical inputs;
+* the batched uneven-size ensemble vs independent lattices per run;
+* the autotuner: state preserved, choices cached and reused.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from helpers import L, random_state
+
+pytestmark = pytest.mark.gpu
+
+
+def _lattice(engine, cfg, separable=True):
+    cfg.spectral_impl = L.SPEC_IMPL_SEPARABLE if separable else L.SPEC_IMPL_CUFFT
+    g = engine.Lattice(cfg)
+    assert g.tuning()[5] == cfg.spectral_impl
+    return g
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 32, 16), (16, 64, 128)])
+@pytest.mark.parametrize("nf", [1, 2])
+@pytest.mark.parametrize("conf", [False, True])
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32_KAHAN])
+def test_separable_vs_cufft(engine, shape, nf, conf, prec):
+    c = L.make_config(shape, nfld=nf, length=0.5 * shape[0], laplacian=L.LAP_SPECTRAL,
+                      background=L.BG_CONFORMAL if conf else L.BG_MINKOWSKI, precision=prec,
+                      model=L.MODEL_PHI4_G2 if nf == 2 else L.MODEL_PHI4,
+                      model_params=(1.0, 2.0) if nf == 2 else (1.0,))
+    a = _lattice(engine, c, True)
+    b = _lattice(engine, c, False)
+    f, p = random_state((nf, shape[2], shape[1], shape[0]), seed=3, mean=1.0, amp=0.05)
+    for g in (a, b):
+        g.set_state(f, p)
+        if conf:
+            g.set_scale_factor(1.0, 0.0)
+            g.calc_metric()
+        g.symp(4, 0.02, 5)
+    fa, pa = a.get_state()
+    fb, pb = b.get_state()
+    tol = 1e-12 if prec == L.FP64 else 2e-6
+    assert rel_err(fa, fb) <= tol
+    assert rel_err(pa, pb) <= tol * 10
+    if conf:
+        (aa, apa), (ab, apb) = a.scale_factor(), b.scale_factor()
+        assert abs(aa - ab) <= tol * ab
+        assert abs(apa - apb) <= tol * 10 * abs(apb)
+
+
+def test_ensemble_matches_single_runs(engine):
+    sizes = [16, 24, 16, 32]
+    base = L.make_config(16, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=L.FP64, model=L.MODEL_PHI4)
+    ens = engine.Ensemble(base, sizes)
+    seeds = [3000 + r for r in range(len(sizes))]
+    ens.init_vacuum(seeds, 1.0, 0.0, 3.0, amp=1e-4, kcut_frac=0.5)
+    ens.symp(4, 1.0 / 20, 6)
+    ens.sync()
+    E = ens.energies()
+    for r, n in enumerate(sizes):
+        c = L.make_config(n, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=L.FP64, model=L.MODEL_PHI4)
+        g = engine.Lattice(c)
+        g.init_vacuum(seeds[r], [1.0], [0.0], [3.0], amp=1e-4, kcut_frac=0.5)
+        g.symp(4, (20.0 / n) / 20, 6)
+        f, p = g.get_state()
+        ef, ep = ens.state(r)
+        assert rel_err(ef, f[0]) <= 1e-12, (r, n)
+        assert rel_err(ep, p[0]) <= 1e-11, (r, n)
+        e = g.energies()
+        assert abs(E[r, L.E_RHO] - e[L.E_RHO]) <= 1e-11 * abs(e[L.E_RHO])
+        S1, W1 = ens.spectrum(r, 12)
+        S2, W2 = g.spectrum(L.SPEC_FLD, 0, L.SPEC_WEIGHTED, 12)
+        assert rel_err(S1, S2) <= 1e-10
+
+
+def test_ensemble_fp32_tracks_fp64(engine):
+    sizes = [32, 16]
+    out = {}
+    for prec in (L.FP64, L.FP32_KAHAN):
+        base = L.make_config(16, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=prec, model=L.MODEL_PHI4)
+        ens = engine.Ensemble(base, sizes)
+        ens.init_vacuum([11, 12], 1.0, 0.0, 3.0, amp=1e-8, kcut_frac=0.5)
+        ens.symp(4, 1.0 / 20, 20)
+        out[prec] = [ens.state(r)[0] for r in range(2)]
+    # fluctuations of ~1e-5 around phi = 1: the FP32 field itself resolves them to ~6e-8 / 1e-5
+    for r in range(2):
+        d64 = out[L.FP64][r] - out[L.FP64][r].mean()
+        d32 = out[L.FP32_KAHAN][r] - out[L.FP64][r].mean()
+        assert rel_err(d32, d64) <= 2e-2
+
+
+@pytest.mark.parametrize("kind", ["fd", "spectral"])
+def test_autotune_preserves_state_and_caches(engine, tmp_path, kind):
+    if kind == "fd":
+        c = L.make_config(32, nfld=1, length=8.0, laplacian=L.LAP_FD27, precision=L.FP32_KAHAN,
+                          model=L.MODEL_DOUBLE_WELL, model_params=(0.01,), gw=True, gw_coupling=2.0)
+    else:
+        c = L.make_config(32, nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                          precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g = engine.Lattice(c)
+    f, p = random_state((c.nfld, 32, 32, 32), seed=5)
+    g.set_state(f, p)
+    g.set_scale_factor(1.1, -0.3)
+    before = g.get_state(), g.scale_factor()
+    cache = tmp_path / "tune.jsonl"
+    g.autotune(cache)
+    after = g.get_state(), g.scale_factor()
+    assert np.array_equal(before[0][0], after[0][0]) and np.array_equal(before[0][1], after[0][1])
+    assert before[1] == after[1]
+    t = g.tuning()
+    assert t[1] in (2, 4, 8, 16) and t[3] in (128, 256) and t[4] in (1, 2, 4, 8)
+    assert t[5] in (L.SPEC_IMPL_CUFFT, L.SPEC_IMPL_SEPARABLE)
+    rec = [json.loads(x) for x in cache.read_text().splitlines()]
+    assert len(rec) == 1 and rec[0]["ty"] == t[1]
+    h = engine.Lattice(c)
+    h.autotune(cache)  # reuses the cached choice
+    assert h.tuning() == t
+    assert len(cache.read_text().splitlines()) == 1
+    # evolution with the tuned shapes still matches an untuned handle
+    u = engine.Lattice(c)
+    for obj in (g, u):
+        obj.set_state(f, p)
+        obj.set_scale_factor(1.1, -0.3)
+        obj.symp(2, 0.01, 4)
+    assert rel_err(g.get_state()[0], u.get_state()[0]) <= 1e-6
