@@ -56,6 +56,18 @@ def init_state(obj, seed):
     obj.calc_metric()
 
 
+def ncu_traffic(kernel_class, workload="spectral256_2f_fp32"):
+    """DRAM bytes (read + write) per launch of a kernel class from the committed ncu capture, or None."""
+    p = ROOT / "profiles" / "dram_traffic_256cube.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        f = ln.split()
+        if len(f) >= 4 and not ln.startswith("#") and f[0] == kernel_class and f[1] == workload:
+            return float(f[2]) + float(f[3])
+    return None
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -207,7 +219,9 @@ def run_ours(args):
     K, W = args.steps, args.warmup
     if args.case == "fd-bubbles":
         return run_fd_case(L, args, local)
-    n = args.n
+    if args.case == "closure":
+        return run_closure_case(L, args, local)
+    n = args.n or N_SIDE
     impl = {"auto": L.SPEC_IMPL_AUTO, "cufft": L.SPEC_IMPL_CUFFT, "separable": L.SPEC_IMPL_SEPARABLE}[args.spectral_impl]
     c = workload_config(L, L.FP32_KAHAN, n, impl)
     c.device = local
@@ -221,8 +235,9 @@ def run_ours(args):
         g.autotune(os.environ.get("LAT_TUNE_CACHE"))
     tuning = g.tuning()
 
-    # warm-up
+    # warm-up, and the CUDA graph of the timed call built outside the timed region
     g.symp(4, dt, W)
+    g.prepare_symp(4, dt, K)
     g.sync()
 
     # timed region: exactly K Yoshida-4 steps in one symp4(dt, K) call
@@ -306,8 +321,10 @@ def diagnostics(L, g, args, dt, ms_step):
         avg_s = own[dom]["avg_us"] * 1e-6
         ach = bytes_per[dom] / avg_s / 1e9
         out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                           "frac": ach / hbm, "traffic": None,
-                           "algorithmic_bytes_per_launch": bytes_per[dom]}
+                           "frac": ach / hbm, "traffic": ncu_traffic(dom),
+                           "algorithmic_bytes_per_launch": bytes_per[dom],
+                           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                             "same workload (profiles/dram_traffic_256cube.txt)"}
     # whole step against the byte model of a 3D-FFT design (264.4 B per site-update) and against the
     # bytes the separable passes actually move (3 kicks x 2 fields x 60 B)
     step_bytes = 3 * (2 * (2 * 4 * N + 2 * 8 * (n // 2 + 1) * n * n) + 2 * 28 * N)
@@ -484,7 +501,7 @@ def init_bubbles(g, n):
 
 def run_fd_case(L, args, local):
     """The FD bubble workload alone at side --n (used for profiling captures)."""
-    n = args.n
+    n = args.n or 256
     c = bubble_config(L, n)
     c.device = local
     g = L.Lattice(c)
@@ -505,6 +522,106 @@ def run_fd_case(L, args, local):
     return 0
 
 
+CONV_FLOPS_PER_SITE = {  # tensor-core FLOPs per site as launched (padded channels) and useful
+    "conv1": (27 * 8 * 32 * 2, 27 * 4 * 32 * 2),
+    "conv2": (27 * 32 * 32 * 2, 27 * 32 * 32 * 2),
+    "conv3": (27 * 32 * 8 * 2, 27 * 32 * 2 * 2),
+}
+
+
+def conv_roofline(L, net, n, reps=10):
+    """Per-layer device time of the forward pass on an n^3 lattice and the
+    tensor FLOP rate against the measured dense BF16 peak."""
+    ms = net.time_forward((n, n, n), reps)
+    pk, kind = peaks()
+    peak = float(pk.get("bf16_tflops", 1900.0))
+    N = n ** 3
+    out = {"lattice": n, "pack_ms": ms[0]}
+    for i, name in enumerate(("conv1", "conv2", "conv3")):
+        launched, useful = CONV_FLOPS_PER_SITE[name]
+        t = ms[i + 1] * 1e-3
+        out[name] = {"ms": ms[i + 1], "tflops_launched": N * launched / t / 1e12,
+                     "tflops_useful": N * useful / t / 1e12}
+    tot = sum(ms[1:]) * 1e-3
+    ach = N * sum(v[0] for v in CONV_FLOPS_PER_SITE.values()) / tot / 1e12
+    out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                       "peak_kind": kind + " dense bf16 (cuBLAS burst)",
+                       "note": "mma.sync m16n8k16/m16n8k8 BF16 implicit-GEMM convolutions, FP32 accumulate"}
+    return out
+
+
+def closure_scenario(args, name):
+    """Setup, time window and attach time of a closure scenario."""
+    import importlib as _il
+    C = _il.import_module("lattice-dev_gb300.closure")
+    L = _il.import_module("lattice-dev_gb300")
+    if name == "preheating":
+        # the two-field preheating model from vacuum fluctuations, expanding, conformal units
+        s = C.Setup(n_fine=args.n_fine, n_coarse=args.n or 64)
+        return C, s, args.t_start, args.t_end, args.t_start
+    # UV-rich fluctuations (<dphi^2> ~ 0.08) in Minkowski: the unresolved modes act on the
+    # resolved ones through a mean-field force
+    nf = args.n_fine
+    s = C.Setup(n_fine=nf, n_coarse=args.n or nf // 4, length=nf / 8.0, background=L.BG_MINKOWSKI,
+                kcut_frac=1.0, amp=0.01, units=L.UNITS_PROGRAM)
+    return C, s, 0.5, 8.0, 0.0
+
+
+def run_closure_case(L, args, local):
+    """Learned closure: fine runs -> training data -> training -> held-out evaluation.
+
+    Fine lattice args.n_fine^3 filtered to the coarse lattice (sharp-k), same
+    box.  Prints one JSON line with the data, training and evaluation figures."""
+    C, s, t0w, t1w, t_attach = closure_scenario(args, args.scenario)
+    train_seeds = list(range(100, 100 + args.train_seeds))
+    eval_seeds = list(range(900, 900 + args.eval_seeds))
+    t0 = time.perf_counter()
+    ds = C.generate(s, train_seeds, t0w, t1w, args.snapshots)
+    t_gen = time.perf_counter() - t0
+    net = L.Net(device=local, seed=11)
+    norm = C.fit_norm(s, ds, net)
+    n_hold = max(1, ds.count // 10)
+    order = np.random.default_rng(0).permutation(ds.count)
+    hold, tr = order[:n_hold], order[n_hold:]
+    fe0 = C.force_error(s, ds, net, hold)
+    t0 = time.perf_counter()
+    hist = C.train(s, ds, net, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, lr_end=args.lr / 10)
+    t_train = time.perf_counter() - t0
+    fe1 = C.force_error(s, ds, net, hold)
+    shape = (s.n_coarse,) * 3
+    t0 = time.perf_counter()
+    for _ in range(5):
+        net.train_step(ds.buf, s.stride, tr[:args.batch], shape, 1e-12)
+    t_step = (time.perf_counter() - t0) / 5
+    ev = C.evaluate(s, net, eval_seeds, t1w, every=args.every, t_attach=t_attach)
+    ds.buf.close()
+    summary = {}
+    for nm in ("plain", "closure"):
+        summary[nm] = {
+            "pk_max_rel_err": np.mean([e[nm]["pk_max_rel_err"] for e in ev], axis=0).tolist(),
+            "pk_mean_rel_err": np.mean([e[nm]["pk_mean_rel_err"] for e in ev], axis=0).tolist(),
+            "time_s": float(np.mean([e[nm]["time_s"] for e in ev]))}
+    t_fine = float(np.mean([e["fine_time_s"] for e in ev]))
+    rl = conv_roofline(L, net, 128)
+    print(json.dumps({
+        "metric": "learned closure: P(k) error vs the filtered fine run, and time to solution",
+        "case": "closure", "scenario": args.scenario, "n_fine": s.n_fine, "n_coarse": s.n_coarse,
+        "length": s.length, "background": "conformal" if s.background == L.BG_CONFORMAL else "minkowski",
+        "ic": {"amp": s.amp, "kcut_frac": s.kcut_frac}, "units": "conformal" if s.units else "program",
+        "train_seeds": len(train_seeds), "eval_seeds": len(eval_seeds), "samples": ds.count,
+        "t_window": [t0w, t1w], "t_eval": t1w, "t_attach": t_attach, "every": args.every,
+        "pk_bins": "width 2pi/L up to half the coarse Nyquist wavenumber",
+        "data_gen_s": t_gen, "train_s": t_train, "train_step_ms": 1e3 * t_step, "batch": args.batch,
+        "epochs": args.epochs, "loss_first_last": [hist[0], hist[-1]],
+        "norm": [list(map(float, v)) for v in norm],
+        "heldout_force_err_untrained": list(map(float, fe0)), "heldout_force_err_trained": list(map(float, fe1)),
+        "eval": ev, "summary": summary, "fine_time_s": t_fine,
+        "speedup_closure_vs_fine": t_fine / summary["closure"]["time_s"],
+        "speedup_plain_vs_fine": t_fine / summary["plain"]["time_s"],
+        "conv_forward_128cube": rl}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -522,9 +639,23 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline number only")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--spectral-impl", default="auto", choices=["auto", "cufft", "separable"])
-    ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling cases; the metric is at 256)")
-    ap.add_argument("--case", default="headline", choices=["headline", "fd-bubbles"],
-                    help="fd-bubbles: the 27-point bubble-collision workload with GW sourcing at side --n")
+    ap.add_argument("--n", type=int, default=None,
+                    help="lattice side: headline 256 (other sides for profiling), fd-bubbles 256, closure coarse 64")
+    ap.add_argument("--case", default="headline", choices=["headline", "fd-bubbles", "closure"],
+                    help="fd-bubbles: the 27-point bubble-collision workload with GW sourcing at side --n; "
+                         "closure: learned subgrid closure, fine --n-fine^3 filtered to --n^3")
+    ap.add_argument("--n-fine", type=int, default=256)
+    ap.add_argument("--scenario", default="preheating", choices=["preheating", "hartree"],
+                    help="closure: two-field preheating from vacuum (expanding), or UV-rich fluctuations (Minkowski)")
+    ap.add_argument("--train-seeds", type=int, default=8)
+    ap.add_argument("--eval-seeds", type=int, default=2)
+    ap.add_argument("--t-start", type=float, default=40.0)
+    ap.add_argument("--t-end", type=float, default=120.0)
+    ap.add_argument("--snapshots", type=int, default=17)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--every", type=int, default=3, help="closure: kicks per network evaluation")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

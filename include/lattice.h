@@ -138,6 +138,10 @@ int lat_calc_metric(lat_t* h);
  * and Discrete/Bubble-Collisions/evolve.f90:118-223.  The whole call runs
  * asynchronously on the handle's stream without host synchronisation. */
 int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps);
+/* Builds and caches the CUDA graph that lat_symp(h, order, dt, nsteps) would
+ * replay from the handle's current buffers, without running it (no
+ * reference counterpart: it moves graph capture out of a timed call). */
+int lat_symp_prepare(lat_t* h, int32_t order, double dt, int32_t nsteps);
 /* symp_o2step(dt,w1,w2), hamiltonian_conformal.f90:50-64. */
 int lat_o2step(lat_t* h, double dt, double w1, double w2);
 /* Hamiltonian_Split(dt, hamind), hamiltonian_conformal.f90:66-81 and
@@ -271,6 +275,65 @@ int lat_ens_spectrum(lat_ens_t* e, int32_t run, int32_t nbins, double* S, double
 int lat_ens_download(lat_ens_t* e, int32_t run, double* fld, double* fldp);
 int lat_ens_sync(lat_ens_t* e);
 
+/* ------------------------------------------------- learned subgrid closure */
+/* No reference counterpart.  A coarse lattice evolved with a kick corrected
+ * by a small network: three periodic 3x3x3 convolutions 4 -> 32 -> 32 -> 2
+ * channels with GELU after the first two, BF16 weights and activations,
+ * FP32 accumulation on the tensor cores, FP32 master weights and Adam state.
+ * Inputs are the coarse (phi, chi, pi_phi, pi_chi) of a two-field lattice,
+ * normalised as (x - in_shift) * in_scale; the output o_f gives the force
+ * correction Delta_f = o_f / out_scale_f and the kick uses V'_f - Delta_f:
+ *   pi_f += dt (a^2 lap phi_f - a^4 (V'_f - Delta_f)).
+ * Training data come from lat_coarsen of fine runs: one sample is six
+ * FP32 arrays [6][nz][ny][nx] (phi, chi, pi_phi, pi_chi, Delta_phi,
+ * Delta_chi) and sample s of a batch starts at data + idx[s] * stride.
+ * Lattices: nx a multiple of 16, ny a multiple of 8. */
+typedef struct lat_net_s lat_net_t;
+/* Variables the network sees on a conformal lattice.  PROGRAM: phi, pi and
+ * Delta as evolved.  CONFORMAL: a phi, pi / a and a^3 Delta, which for the
+ * quartic models make the data stationary in the radiation era (the kick
+ * then adds hk a (a^3 Delta)).  Minkowski lattices ignore the choice. */
+enum lat_closure_units { LAT_UNITS_PROGRAM = 0, LAT_UNITS_CONFORMAL = 1 };
+int64_t lat_net_nparams(void);
+int lat_net_create(lat_net_t** out, int32_t device, uint64_t seed);
+int lat_net_destroy(lat_net_t* n);
+/* flat FP32 parameters: W1[27][8][32] b1[32] W2[27][32][32] b2[32]
+ * W3[27][32][8] b3[8]; tap = (dz+1)*9 + (dy+1)*3 + (dx+1) for the input
+ * offset (dx, dy, dz); padded channels (inputs 4..7, outputs 2..7) are zero */
+int lat_net_get_params(lat_net_t* n, float* out, int64_t count);
+int lat_net_set_params(lat_net_t* n, const float* in, int64_t count);
+int lat_net_set_norm(lat_net_t* n, const double in_shift[4], const double in_scale[4],
+                     const double out_scale[2]);
+int lat_net_get_norm(const lat_net_t* n, double in_shift[4], double in_scale[4], double out_scale[2]);
+/* network output (normalised units) of nidx samples into out_dev [nidx][N][2] */
+int lat_net_forward(lat_net_t* n, const float* data_dev, int64_t stride, const int32_t* idx,
+                    int32_t nidx, int32_t nx, int32_t ny, int32_t nz, float* out_dev);
+/* mean squared error of the batch against out_scale * Delta and its gradient
+ * with respect to the flat parameters (grad_host may be NULL); no update */
+int lat_net_grad(lat_net_t* n, const float* data_dev, int64_t stride, const int32_t* idx,
+                 int32_t nidx, int32_t nx, int32_t ny, int32_t nz, double* loss, float* grad_host);
+/* one Adam step (beta 0.9, 0.999, eps 1e-8) on the batch; returns the loss before the step */
+int lat_net_train_step(lat_net_t* n, const float* data_dev, int64_t stride, const int32_t* idx,
+                       int32_t nidx, int32_t nx, int32_t ny, int32_t nz, double lr, double* loss);
+int64_t lat_net_launch_count(const lat_net_t* n);
+/* Device time (CUDA events on the network's stream, after one warm-up) of
+ * one forward pass over an nx x ny x nz lattice, averaged over `reps`:
+ * ms[0] input packing, ms[1..3] the three convolutions. */
+int lat_net_time_forward(lat_net_t* n, int32_t nx, int32_t ny, int32_t nz, int32_t reps, double ms[4]);
+/* Attach (net != NULL) or detach (NULL) a closure to a two-field lattice.
+ * lat_symp then evaluates the network on the current fields before the
+ * first of every `every` kicks of a call (every >= 1) and applies the
+ * correction after each kick; `units` is a lat_closure_units value and must
+ * match the data the network was trained on.  The normalisation is read at
+ * attach time. */
+int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units);
+/* Sharp-k filter of a fine lattice onto a coarse nc^3 lattice of the same
+ * box: modes |k_i| < nc/2 (per axis, coarse Nyquist planes dropped) are kept,
+ * in FP64.  Writes FP32 [3 nf][nc^3]: the filtered fields, the filtered
+ * momenta, and Delta_f = V'_f(F phi) - F V'_f(phi) (the force the coarse
+ * kick misses) into out_dev, in the variables `units` selects. */
+int lat_coarsen(lat_t* fine, int32_t nc, int32_t units, float* out_dev);
+
 /* ---------------------------------------------------------- measurement */
 /* Kernel classes timed with CUDA events on the handle's stream when
  * timing is enabled (one event pair per launch). */
@@ -305,6 +368,11 @@ int lat_device_ptr(lat_t* h, int32_t what, void** ptr);
 /* Pinned host memory for staging (cudaHostAlloc / cudaFreeHost). */
 int lat_host_alloc(void** ptr, size_t bytes);
 int lat_host_free(void* ptr);
+/* Device memory for data sets (closure training samples) and a synchronous
+ * copy; kind 0 host to device, 1 device to host, 2 device to device. */
+int lat_dev_alloc(int32_t device, void** ptr, size_t bytes);
+int lat_dev_free(void* ptr);
+int lat_memcpy(void* dst, const void* src, size_t bytes, int32_t kind);
 
 /* -------------------------------------------------------------- autotune */
 /* Times the candidate tile shapes / block schedules of this handle's kernels

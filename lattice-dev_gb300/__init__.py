@@ -42,6 +42,7 @@ MODEL_PHI4, MODEL_PHI4_G2, MODEL_DOUBLE_WELL, MODEL_FREE = 0, 1, 2, 3
 SPEC_FLD, SPEC_FLDP = 0, 1
 SPEC_WEIGHTED, SPEC_COUNT = 0, 1
 SPEC_IMPL_AUTO, SPEC_IMPL_CUFFT, SPEC_IMPL_SEPARABLE = 0, 1, 2
+UNITS_PROGRAM, UNITS_CONFORMAL = 0, 1  # closure variables (lat_closure_units)
 E_KE, E_GE_LAP, E_GE_GRAD, E_PE, E_RHO, E_GRAV, E_RESIDUAL, E_A, E_AP, E_MEAN0, E_MEAN1, E_GW = range(12)
 NENERGY = 12
 K_KICKDRIFT, K_DRIFT, K_KICK, K_KMUL, K_FFT_R2C, K_FFT_C2R, K_GW, K_OTHER, K_SEP_X, K_SEP_Y, K_SEP_Z = range(11)
@@ -93,7 +94,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_get_config": ([P, C.POINTER(LatConfig)], I),
         "lat_upload": ([P, dp, I, I, dp, I, I], I), "lat_download": ([P, dp, I, I, dp, I, I], I),
         "lat_set_scale_factor": ([P, D, D], I), "lat_get_scale_factor": ([P, dp, dp], I),
-        "lat_calc_metric": ([P], I), "lat_symp": ([P, I, D, I], I), "lat_o2step": ([P, D, D, D], I),
+        "lat_calc_metric": ([P], I), "lat_symp": ([P, I, D, I], I), "lat_symp_prepare": ([P, I, D, I], I), "lat_o2step": ([P, D, D, D], I),
         "lat_split": ([P, D, I], I), "lat_get_time": ([P, dp], I), "lat_sync": ([P], I),
         "lat_laplacian": ([P, I, dp], I), "lat_laplacian_3d": ([I, I, I, dp, D], I),
         "lat_energies": ([P, dp], I), "lat_spectrum_nbins": ([P, C.POINTER(I)], I),
@@ -115,6 +116,17 @@ def _declare(lib: C.CDLL) -> None:
         "lat_device_ptr": ([P, I, C.POINTER(P)], I), "lat_host_alloc": ([C.POINTER(P), C.c_size_t], I),
         "lat_host_free": ([P], I), "lat_autotune": ([P, C.c_char_p], I),
         "lat_tuning_get": ([P, C.POINTER(I)], I),
+        "lat_dev_alloc": ([I, C.POINTER(P), C.c_size_t], I), "lat_dev_free": ([P], I),
+        "lat_memcpy": ([P, P, C.c_size_t, I], I),
+        "lat_net_nparams": ([], I64), "lat_net_create": ([C.POINTER(P), I, U64], I), "lat_net_destroy": ([P], I),
+        "lat_net_get_params": ([P, C.POINTER(C.c_float), I64], I),
+        "lat_net_set_params": ([P, C.POINTER(C.c_float), I64], I),
+        "lat_net_set_norm": ([P, dp, dp, dp], I), "lat_net_get_norm": ([P, dp, dp, dp], I),
+        "lat_net_forward": ([P, P, I64, C.POINTER(I), I, I, I, I, P], I),
+        "lat_net_grad": ([P, P, I64, C.POINTER(I), I, I, I, I, dp, C.POINTER(C.c_float)], I),
+        "lat_net_train_step": ([P, P, I64, C.POINTER(I), I, I, I, I, D, dp], I),
+        "lat_net_launch_count": ([P], I64), "lat_net_time_forward": ([P, I, I, I, I, dp], I),
+        "lat_closure_attach": ([P, P, I, I], I), "lat_coarsen": ([P, I, I, P], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name, None)
@@ -229,6 +241,10 @@ class Lattice:
     # integrator ----------------------------------------------------------------
     def symp(self, order: int, dt: float, nsteps: int) -> None:
         _check(_lib.lat_symp(self._h, order, dt, nsteps))
+
+    def prepare_symp(self, order: int, dt: float, nsteps: int) -> None:
+        """Capture (not run) the CUDA graph of symp(order, dt, nsteps)."""
+        _check(_lib.lat_symp_prepare(self._h, order, dt, nsteps))
 
     def symp2(self, dt, nsteps):
         self.symp(2, dt, nsteps)
@@ -363,6 +379,139 @@ class Lattice:
         out = (C.c_int32 * 6)()
         _check(_lib.lat_tuning_get(self._h, out))
         return list(out)
+
+    # learned closure
+    def coarsen(self, nc: int, out: "DeviceArray", offset: int = 0, units: int = 0) -> None:
+        """Sharp-k filtered fields, momenta and missing forces on an nc^3 lattice,
+        written as FP32 [3 nf][nc^3] at element `offset` of `out`."""
+        offset, nc = int(offset), int(nc)
+        if offset < 0 or offset + 3 * self.nfld * nc ** 3 > out.size:
+            raise ValueError("coarsen output does not fit")
+        _check(_lib.lat_coarsen(self._h, nc, units, out.ptr + 4 * offset))
+
+    def attach_closure(self, net: "Net | None", every: int = 1, units: int = 0) -> None:
+        _check(_lib.lat_closure_attach(self._h, None if net is None else net._h, every, units))
+        self._closure = net  # keeps the network alive while attached
+
+
+class DeviceArray:
+    """A flat FP32 device buffer (lat_dev_alloc) for closure data sets."""
+
+    def __init__(self, size: int, device: int = 0):
+        load_library()
+        self.size = int(size)
+        p = C.c_void_p()
+        _check(_lib.lat_dev_alloc(device, C.byref(p), 4 * self.size))
+        self.ptr = p.value
+
+    def upload(self, a: np.ndarray, offset: int = 0) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        offset = int(offset)
+        if offset < 0 or offset + a.size > self.size:
+            raise ValueError("upload out of range")
+        _check(_lib.lat_memcpy(self.ptr + 4 * offset, a.ctypes.data, 4 * a.size, 0))
+
+    def download(self, count: int | None = None, offset: int = 0) -> np.ndarray:
+        offset = int(offset)
+        count = self.size - offset if count is None else int(count)
+        if offset < 0 or offset + count > self.size:
+            raise ValueError("download out of range")
+        out = np.empty(count, dtype=np.float32)
+        _check(_lib.lat_memcpy(out.ctypes.data, self.ptr + 4 * offset, 4 * count, 1))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            _lib.lat_dev_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Net:
+    """The closure network (lat_net_*): 4 -> 32 -> 32 -> 2 periodic 3^3 convolutions."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        load_library()
+        self._h = C.c_void_p()
+        _check(_lib.lat_net_create(C.byref(self._h), device, seed))
+        self.nparams = int(_lib.lat_net_nparams())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lat_net_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparams, dtype=np.float32)
+        _check(_lib.lat_net_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), self.nparams))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(_lib.lat_net_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size))
+
+    def set_norm(self, shift, scale, out_scale) -> None:
+        a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (shift, scale, out_scale))
+        _check(_lib.lat_net_set_norm(self._h, _dp(a), _dp(b), _dp(c)))
+
+    def norm(self):
+        a, b, c = np.zeros(4), np.zeros(4), np.zeros(2)
+        _check(_lib.lat_net_get_norm(self._h, _dp(a), _dp(b), _dp(c)))
+        return a, b, c
+
+    @staticmethod
+    def _idx(idx):
+        i = np.ascontiguousarray(idx, dtype=np.int32)
+        return i, i.ctypes.data_as(C.POINTER(C.c_int32))
+
+    def forward(self, data: DeviceArray, stride: int, idx, shape) -> np.ndarray:
+        i, ip = self._idx(idx)
+        nx, ny, nz = (int(v) for v in shape)
+        stride = int(stride)
+        out = DeviceArray(len(i) * nx * ny * nz * 2)
+        _check(_lib.lat_net_forward(self._h, data.ptr, stride, ip, len(i), nx, ny, nz, out.ptr))
+        r = out.download().reshape(len(i), nz, ny, nx, 2)
+        out.close()
+        return r
+
+    def grad(self, data: DeviceArray, stride: int, idx, shape):
+        i, ip = self._idx(idx)
+        nx, ny, nz = (int(v) for v in shape)
+        stride = int(stride)
+        loss = C.c_double()
+        g = np.empty(self.nparams, dtype=np.float32)
+        _check(_lib.lat_net_grad(self._h, data.ptr, stride, ip, len(i), nx, ny, nz, C.byref(loss),
+                                 g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    def train_step(self, data: DeviceArray, stride: int, idx, shape, lr: float) -> float:
+        i, ip = self._idx(idx)
+        nx, ny, nz = (int(v) for v in shape)
+        stride = int(stride)
+        loss = C.c_double()
+        _check(_lib.lat_net_train_step(self._h, data.ptr, stride, ip, len(i), nx, ny, nz, lr, C.byref(loss)))
+        return loss.value
+
+    def launch_count(self) -> int:
+        return int(_lib.lat_net_launch_count(self._h))
+
+    def time_forward(self, shape, reps: int = 10) -> np.ndarray:
+        """ms of (input packing, conv1, conv2, conv3) on an nx x ny x nz lattice."""
+        nx, ny, nz = (int(v) for v in shape)
+        ms = np.zeros(4)
+        _check(_lib.lat_net_time_forward(self._h, nx, ny, nz, reps, _dp(ms)))
+        return ms
 
 
 class Ensemble:

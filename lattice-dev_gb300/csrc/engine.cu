@@ -24,6 +24,7 @@
 
 #include "engine.hpp"
 #include "integrator.hpp"
+#include "net.hpp"
 
 namespace lat {
 
@@ -141,6 +142,13 @@ struct lat_s {
   cudaEvent_t marks[16] = {};
   bool use_graphs = true;
   std::vector<GraphEntry> graphs;
+
+  // learned closure (lat_closure_attach)
+  lat_net_s* cl_net = nullptr;
+  int cl_every = 1;
+  int cl_units = 0;  // 1: the network sees (a phi, pi / a) and predicts a^3 Delta
+  double cl_tscale[2] = {1, 1};
+  net::InferBufs cl_b{};
 };
 
 namespace {
@@ -401,6 +409,9 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
   a.pi_out = h->fldp_alt;
   a.lap_out = axis == 0 ? h->lap : h->lap_alt;
   a.twN = h->tw[axis];
+  if (!h->sep_ok || !a.twN || !a.phi || !a.phi_out || !a.pi || !a.pi_out || !a.lap || !a.lap_out ||
+      (h->prec == LAT_FP32_KAHAN && (!a.phic || !a.phic_out)))
+    return set_error(LAT_ERR_STATE, "separable pass buffers missing");
   const int n = axis == 0 ? h->nx : (axis == 1 ? h->ny : h->nz);
   const double dk = axis == 0 ? h->dkx : (axis == 1 ? h->dky : h->dkz);
   a.dk2 = dk * dk;
@@ -475,10 +486,50 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
   return LAT_OK;
 }
 
+// Op list with the closure: plain passes, the network evaluated on the
+// fields before the first of every cl_every kicks, and its force correction
+// applied after each kick (the kick itself is unchanged).
+int exec_closure(lat_s* h, const std::vector<Op>& ops) {
+  int kicks = 0;
+  for (const Op& o : ops) {
+    switch (o.t) {
+      case 'D': RET(exec_drift(h, o.h)); break;
+      case 'G': RET(exec_grav(h, o.h)); break;
+      case 'K': {
+        if (kicks % h->cl_every == 0) {
+          Timed t(h, LAT_K_OTHER);
+          const size_t fb = (size_t)h->N * h->rsz;
+          const void* ch[4] = {h->fld[h->cur], (const char*)h->fld[h->cur] + fb, h->fldp, (const char*)h->fldp + fb};
+          RET(net::infer(h->cl_net, ch, h->prec == LAT_FP64 ? 1 : 0, h->nx, h->ny, h->nz,
+                         h->cl_units ? h->sc : nullptr, h->cl_b, h->stream));
+        }
+        ++kicks;
+        RET(exec_kick(h, o.h));
+        Timed t(h, LAT_K_OTHER);
+        net::CorrArgs c{};
+        c.pi = h->fldp;
+        c.out = h->cl_b.out;
+        c.tscale[0] = h->cl_tscale[0];
+        c.tscale[1] = h->cl_tscale[1];
+        c.hk = o.h;
+        c.conf = conformal(h) ? 1 : 0;
+        c.units = h->cl_units;
+        c.sc = h->sc;
+        c.N = h->N;
+        RET(net::corr_kick(c, h->prec == LAT_FP64 ? 1 : 0, h->nsm, h->stream));
+        break;
+      }
+      default: break;
+    }
+  }
+  return LAT_OK;
+}
+
 int exec_fused(lat_s* h, const std::vector<Op>& in) {
   std::vector<Op> ops;
   for (const Op& o : in)
     if (o.t != 'M') ops.push_back(o);
+  if (h->cl_net) return exec_closure(h, ops);
   const bool conf = conformal(h);
   if (h->sep && (!conf || h->cfg.split_order == LAT_SPLIT_PSEUDOSPEC)) {
     const int st = exec_sep(h, ops);
@@ -681,6 +732,90 @@ int output_spectrum(lat_s* h, int what, int field, int slot, void** Fout, int* p
 
 }  // namespace
 
+namespace {
+// lat_symp through the handle's graph cache.  run = false builds and caches
+// the graph of the call without launching it (the handle's state is left
+// as it was).
+int symp_graph(lat_s* h, int32_t order, double dt, int32_t nsteps, bool run) {
+  std::vector<Op> ops;
+  double tg[3] = {h->tglobal[0], h->tglobal[1], h->tglobal[2]};
+  Emitter em = emitter(h, &ops, tg);
+  RET(em.symp(order, dt, nsteps));
+  const bool graphs = h->use_graphs && !h->timing;
+  if (!graphs) {
+    if (!run) return LAT_OK;
+    RET(exec_fused(h, ops));
+    std::memcpy(h->tglobal, tg, sizeof(tg));
+    return LAT_OK;
+  }
+  for (auto& ge : h->graphs) {
+    if (ge.order == order && ge.dt == dt && ge.nsteps == nsteps && ge.cur == h->cur && ge.ucur == h->ucur &&
+        ge.fldc == h->fldc && ge.fldp == h->fldp) {
+      if (!run) return LAT_OK;
+      CK(cudaGraphLaunch(ge.exec, h->stream));
+      h->launches += ge.kernels;
+      h->cur = ge.cur_after;
+      h->ucur = ge.ucur_after;
+      if (h->fldc != ge.fldc_after) std::swap(h->fldc, h->fldc_alt);
+      if (h->fldp != ge.fldp_after) std::swap(h->fldp, h->fldp_alt);
+      std::memcpy(h->tglobal, tg, sizeof(tg));
+      return LAT_OK;
+    }
+  }
+  GraphEntry ge{};
+  ge.order = order; ge.dt = dt; ge.nsteps = nsteps; ge.cur = h->cur; ge.ucur = h->ucur;
+  ge.fldc = h->fldc; ge.fldp = h->fldp;
+  void* const c_alt0 = h->fldc_alt;
+  void* const p_alt0 = h->fldp_alt;
+  const int64_t before = h->launches;
+  auto rewind = [&]() {  // pointer state before the capture
+    h->cur = ge.cur; h->ucur = ge.ucur;
+    h->fldc = ge.fldc; h->fldc_alt = c_alt0;
+    h->fldp = ge.fldp; h->fldp_alt = p_alt0;
+  };
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+  int st = exec_fused(h, ops);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (st != LAT_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    rewind();
+    h->launches = before;
+    return st;
+  }
+  if (e != cudaSuccess) {
+    rewind();
+    h->launches = before;
+    return cuda_fail(e, "graph capture");
+  }
+  ge.kernels = h->launches - before;
+  ge.cur_after = h->cur;
+  ge.ucur_after = h->ucur;
+  ge.fldc_after = h->fldc;
+  ge.fldp_after = h->fldp;
+  e = cudaGraphInstantiate(&ge.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    rewind();
+    h->launches = before;
+    return cuda_fail(e, "graph instantiate");
+  }
+  if (h->graphs.size() >= 8) {
+    cudaGraphExecDestroy(h->graphs.front().exec);
+    h->graphs.erase(h->graphs.begin());
+  }
+  h->graphs.push_back(ge);
+  if (!run) {  // nothing ran: the handle keeps its state
+    rewind();
+    h->launches = before;
+    return LAT_OK;
+  }
+  CK(cudaGraphLaunch(ge.exec, h->stream));
+  std::memcpy(h->tglobal, tg, sizeof(tg));
+  return LAT_OK;
+}
+}  // namespace
+
 // ====================================================================== C ABI
 extern "C" {
 
@@ -694,6 +829,11 @@ int lat_destroy(lat_t* h) {
   free_graphs(h);
   for (void* t : h->tw)
     if (t) cudaFree(t);
+  {
+    void* cb[] = {h->cl_b.a0, h->cl_b.a1, h->cl_b.a2, h->cl_b.out};
+    for (void* b : cb)
+      if (b) cudaFree(b);
+  }
   if (h->Fk64) cudaFree(h->Fk64);
   if (h->have_d2z1) cufftDestroy(h->p_d2z1);
   void* bufs[] = {h->fld[0], h->fld[1], h->fldc, h->fldp, h->lap, h->fldc_alt, h->fldp_alt, h->lap_alt, h->Fk,
@@ -837,7 +977,7 @@ int lat_create(lat_t** out, const lat_config* cfg) {
       if ((st = alloc(&h->fldp_alt, fb))) return bail(st);
       if ((st = alloc(&h->lap_alt, fb))) return bail(st);
     }
-    if (h->sep) {
+    if (h->sep_ok) {  // the autotuner may switch an AUTO handle to the passes later
       const int dims[3] = {h->nx, h->ny, h->nz};
       for (int ax = 0; ax < 3; ++ax) {
         const int n = dims[ax];
@@ -976,63 +1116,13 @@ int lat_o2step(lat_t* h, double dt, double w1, double w2) {
 int lat_symp(lat_t* h, int32_t order, double dt, int32_t nsteps) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
-  std::vector<Op> ops;
-  double tg[3] = {h->tglobal[0], h->tglobal[1], h->tglobal[2]};
-  Emitter em = emitter(h, &ops, tg);
-  RET(em.symp(order, dt, nsteps));
-  const bool graphs = h->use_graphs && !h->timing;
-  if (!graphs) {
-    RET(exec_fused(h, ops));
-    std::memcpy(h->tglobal, tg, sizeof(tg));
-    return LAT_OK;
-  }
-  for (auto& ge : h->graphs) {
-    if (ge.order == order && ge.dt == dt && ge.nsteps == nsteps && ge.cur == h->cur && ge.ucur == h->ucur &&
-        ge.fldc == h->fldc && ge.fldp == h->fldp) {
-      CK(cudaGraphLaunch(ge.exec, h->stream));
-      h->launches += ge.kernels;
-      h->cur = ge.cur_after;
-      h->ucur = ge.ucur_after;
-      if (h->fldc != ge.fldc_after) std::swap(h->fldc, h->fldc_alt);
-      if (h->fldp != ge.fldp_after) std::swap(h->fldp, h->fldp_alt);
-      std::memcpy(h->tglobal, tg, sizeof(tg));
-      return LAT_OK;
-    }
-  }
-  GraphEntry ge{};
-  ge.order = order; ge.dt = dt; ge.nsteps = nsteps; ge.cur = h->cur; ge.ucur = h->ucur;
-  ge.fldc = h->fldc; ge.fldp = h->fldp;
-  void* const c_alt0 = h->fldc_alt;
-  void* const p_alt0 = h->fldp_alt;
-  const int64_t before = h->launches;
-  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
-  int st = exec_fused(h, ops);
-  cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
-  if (st != LAT_OK) {
-    if (graph) cudaGraphDestroy(graph);
-    h->cur = ge.cur; h->ucur = ge.ucur;
-    h->fldc = ge.fldc; h->fldc_alt = c_alt0;
-    h->fldp = ge.fldp; h->fldp_alt = p_alt0;
-    return st;
-  }
-  if (e != cudaSuccess) return cuda_fail(e, "graph capture");
-  ge.kernels = h->launches - before;
-  ge.cur_after = h->cur;
-  ge.ucur_after = h->ucur;
-  ge.fldc_after = h->fldc;
-  ge.fldp_after = h->fldp;
-  e = cudaGraphInstantiate(&ge.exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
-  if (h->graphs.size() >= 8) {
-    cudaGraphExecDestroy(h->graphs.front().exec);
-    h->graphs.erase(h->graphs.begin());
-  }
-  h->graphs.push_back(ge);
-  CK(cudaGraphLaunch(ge.exec, h->stream));
-  std::memcpy(h->tglobal, tg, sizeof(tg));
-  return LAT_OK;
+  return symp_graph(h, order, dt, nsteps, true);
+}
+
+int lat_symp_prepare(lat_t* h, int32_t order, double dt, int32_t nsteps) {
+  if (!h) return set_error(LAT_ERR_ARG, "null handle");
+  ApiGuard g(h);
+  return symp_graph(h, order, dt, nsteps, false);
 }
 
 int lat_get_time(lat_t* h, double tglobal[3]) {
@@ -1396,6 +1486,24 @@ int lat_host_free(void* ptr) {
   return LAT_OK;
 }
 
+int lat_dev_alloc(int32_t device, void** ptr, size_t bytes) {
+  if (!ptr) return set_error(LAT_ERR_ARG, "null argument");
+  cudaSetDevice(device);
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  return e == cudaSuccess ? LAT_OK : set_error(LAT_ERR_ALLOC, cudaGetErrorString(e));
+}
+int lat_dev_free(void* ptr) {
+  if (ptr) cudaFree(ptr);
+  return LAT_OK;
+}
+int lat_memcpy(void* dst, const void* src, size_t bytes, int32_t kind) {
+  if ((!dst || !src) && bytes) return set_error(LAT_ERR_ARG, "null argument");
+  if (kind < 0 || kind > 2) return set_error(LAT_ERR_ARG, "kind: 0 host to device, 1 device to host, 2 device to device");
+  const cudaMemcpyKind k[3] = {cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice};
+  cudaError_t e = cudaMemcpy(dst, src, bytes, k[kind]);
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "lat_memcpy");
+}
+
 int lat_laplacian_3d(int32_t n1, int32_t n2, int32_t n3, double* f, double dk) {
   if (!f || n1 < 2 || n2 < 2 || n3 < 2 || !(dk > 0)) return set_error(LAT_ERR_ARG, "bad laplacian_3d arguments");
   lat_config c{};
@@ -1620,6 +1728,111 @@ int lat_autotune(lat_t* h, const char* cache_path) {
     }
   }
   return LAT_OK;
+}
+
+int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
+  if (!h) return set_error(LAT_ERR_ARG, "null handle");
+  ApiGuard g(h);
+  CK(cudaStreamSynchronize(h->stream));
+  free_graphs(h);
+  if (!net) {
+    h->cl_net = nullptr;
+    return LAT_OK;
+  }
+  if (h->nf != 2) return set_error(LAT_ERR_UNSUPPORTED, "the closure network takes two fields");
+  if (h->nx % 16 || h->ny % 8) return set_error(LAT_ERR_UNSUPPORTED, "closure lattice: nx % 16 == 0, ny % 8 == 0");
+  if (every < 1) return set_error(LAT_ERR_ARG, "every must be >= 1");
+  if (units != LAT_UNITS_PROGRAM && units != LAT_UNITS_CONFORMAL) return set_error(LAT_ERR_ARG, "units: 0 or 1");
+  if (net::net_device(net) != h->dev) return set_error(LAT_ERR_ARG, "network and lattice on different devices");
+  if (!h->cl_b.a0) {
+    CK(cudaMalloc(&h->cl_b.a0, (size_t)h->N * net::C_IN * 2));
+    CK(cudaMalloc(&h->cl_b.a1, (size_t)h->N * net::C_HID * 2));
+    CK(cudaMalloc(&h->cl_b.a2, (size_t)h->N * net::C_HID * 2));
+    CK(cudaMalloc(&h->cl_b.out, (size_t)h->N * 2 * sizeof(float)));
+  }
+  h->cl_net = net;
+  h->cl_every = every;
+  h->cl_units = conformal(h) ? units : LAT_UNITS_PROGRAM;  // a = 1 in Minkowski
+  net::out_scale(net, h->cl_tscale);
+  return LAT_OK;
+}
+
+int lat_coarsen(lat_t* h, int32_t nc, int32_t units, float* out) {
+  if (!h || !out) return set_error(LAT_ERR_ARG, "null argument");
+  ApiGuard g(h);
+  if (units != LAT_UNITS_PROGRAM && units != LAT_UNITS_CONFORMAL) return set_error(LAT_ERR_ARG, "units: 0 or 1");
+  double av = 1.0;  // conformal units: fields times a, momenta over a, Delta times a^3
+  if (units == LAT_UNITS_CONFORMAL && conformal(h)) {
+    DevScalars scal{};
+    RET(read_scalars(h, &scal));
+    av = scal.a;
+  }
+  if (nc < 4 || nc % 2 || nc > h->nx || nc > h->ny || nc > h->nz)
+    return set_error(LAT_ERR_ARG, "coarse side: even, at least 4, at most the fine sides");
+  if (h->nx % 2) return set_error(LAT_ERR_ARG, "fine nx must be even");
+  const int64_t Nc = (int64_t)nc * nc * nc, Mc = (int64_t)(nc / 2 + 1) * nc * nc;
+  const int nf = h->nf;
+  RET(ensure_stage(h, (size_t)std::max(nf, 2) * h->N));
+  if (!h->Fk64) CK(cudaMalloc(&h->Fk64, (size_t)2 * h->M * sizeof(double2)));
+  if (h->prec != LAT_FP64 && !h->have_d2z1) {
+    CF(cufftCreate(&h->p_d2z1));
+    int n[3] = {h->nz, h->ny, h->nx};
+    size_t ws = 0;
+    CF(cufftMakePlanMany(h->p_d2z1, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1, &ws));
+    CF(cufftSetStream(h->p_d2z1, h->stream));
+    h->have_d2z1 = true;
+  }
+  double2* Fc = nullptr;
+  double *phic = nullptr, *tmp = nullptr;
+  cufftHandle pc = 0;
+  bool have_pc = false;
+  int st = LAT_OK;
+  auto fine_fft = [&](const double* in) -> int {  // fine FP64 real -> Fk64
+    if (h->prec == LAT_FP64) return fft_exec_r2c(h, h->p_r2c1, in, h->Fk64);
+    CF(cufftExecD2Z(h->p_d2z1, const_cast<double*>(in), (cufftDoubleComplex*)h->Fk64));
+    return LAT_OK;
+  };
+  auto filter = [&](const double* in, double* dst) -> int {  // fine real -> coarse real (FP64)
+    RET(fine_fft(in));
+    RET(launch_truncate((const double2*)h->Fk64, h->nx, h->ny, h->nz, Fc, nc, 1.0 / (double)h->N, h->stream));
+    CF(cufftExecZ2D(pc, (cufftDoubleComplex*)Fc, dst));
+    return LAT_OK;
+  };
+  auto body = [&]() -> int {
+    CK(cudaMalloc(&Fc, (size_t)Mc * sizeof(double2)));
+    CK(cudaMalloc(&phic, (size_t)nf * Nc * sizeof(double)));
+    CK(cudaMalloc(&tmp, (size_t)Nc * sizeof(double)));
+    CF(cufftPlan3d(&pc, nc, nc, nc, CUFFT_Z2D));
+    have_pc = true;
+    CF(cufftSetStream(pc, h->stream));
+    double* fine = h->stage;
+    const size_t fb = (size_t)h->N * h->rsz;
+    for (int f = 0; f < nf; ++f) {  // filtered fields (kept in FP64 for Delta)
+      const void* comp = h->fldc ? (const char*)h->fldc + f * fb : nullptr;
+      RET(launch_to_fp64((const char*)h->fld[h->cur] + f * fb, comp, h->N, h->prec, fine, h->stream));
+      RET(filter(fine, phic + f * Nc));
+      RET(launch_to_f32(phic + f * Nc, Nc, av, out + (int64_t)f * Nc, h->stream));
+    }
+    for (int f = 0; f < nf; ++f) {  // filtered momenta
+      RET(launch_to_fp64((const char*)h->fldp + f * fb, nullptr, h->N, h->prec, fine, h->stream));
+      RET(filter(fine, tmp));
+      RET(launch_to_f32(tmp, Nc, 1.0 / av, out + (int64_t)(nf + f) * Nc, h->stream));
+    }
+    RET(launch_dv_fine(h->fld[h->cur], h->fldc, nf, h->N, model_of(h), h->prec, fine, h->stream));
+    for (int f = 0; f < nf; ++f) {  // Delta_f = V'_f(F phi) - F V'_f(phi)
+      RET(filter(fine + (size_t)f * h->N, tmp));
+      RET(launch_delta(phic, tmp, f, nf, Nc, model_of(h), av * av * av, out + (int64_t)(2 * nf + f) * Nc, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return LAT_OK;
+  };
+  st = body();
+  cudaStreamSynchronize(h->stream);
+  if (have_pc) cufftDestroy(pc);
+  if (Fc) cudaFree(Fc);
+  if (phic) cudaFree(phic);
+  if (tmp) cudaFree(tmp);
+  return st;
 }
 
 int lat_tuning_get(const lat_t* h, int32_t out[6]) {

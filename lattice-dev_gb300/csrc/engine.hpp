@@ -185,6 +185,14 @@ int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStre
 int launch_bubbles(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* centres_dev,
                    double radius, double width, cudaStream_t s);
 
+// ------------------------------------------- coarsening (k_coarse.cu)
+int launch_truncate(const double2* Ff, int fnx, int fny, int fnz, double2* Fc, int nc, double scale, cudaStream_t s);
+int launch_dv_fine(const void* fld, const void* c, int nf, int64_t N, const ModelP& m, int precision, double* out,
+                   cudaStream_t s);
+int launch_delta(const double* phic, const double* filt, int f, int nf, int64_t Nc, const ModelP& m, double scale,
+                 float* out, cudaStream_t s);
+int launch_to_f32(const double* in, int64_t n, double scale, float* out, cudaStream_t s);
+
 // bookkeeping of launches for the kernel-launch census
 extern thread_local int64_t* g_launch_counter;
 

@@ -1,0 +1,600 @@
+// k_net.cu -- BF16 kernels of the learned subgrid closure (sm_103a).
+//
+// The closure network is three periodic 3x3x3 convolutions, 4 -> 32 -> 32 -> 2
+// channels, GELU after the first two.  Activations are stored channels-last
+// ([lattice][z][y][x][C], C padded to 8 or 32) in BF16; every product
+// accumulates in FP32 on the tensor cores (mma.sync m16n8k16 / m16n8k8 with
+// BF16 operands); the master weights and the optimiser state are FP32.
+//
+// A convolution is an implicit GEMM: output sites x output channels, summed
+// over 27 taps x input channels.  A block stages its tile's input halo and
+// all 27 weight taps in shared memory and walks the taps with ldmatrix; the
+// same kernel runs the backward data pass with the taps mirrored and the
+// weights transposed.  The weight gradient is a GEMM over sites: per block
+// partial sums, reduced over blocks in a fixed order (deterministic).
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "net.hpp"
+
+namespace lat {
+namespace net {
+
+namespace {
+
+constexpr int TX = 16, TY = 8, HX = TX + 2, HY = TY + 2, HZ = 3, HSITES = HX * HY * HZ;
+constexpr int TSITES = TX * TY;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp16(void* s, const void* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(s)), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x1(uint32_t& r, const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x1.shared.b16 {%0}, [%1];\n" : "=r"(r) : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(smem_u32(p)));
+}
+// D = A(16x16, row) B(16x8, col) + D, BF16 in, FP32 accumulate
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+// D = A(16x8, row) B(8x8, col) + D
+__device__ __forceinline__ void mma1688(float (&d)[4], const uint32_t (&a)[2], uint32_t b0) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};\n"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(b0));
+}
+
+// GELU with the error function, and its derivative
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z) {
+  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// padded shared-memory row (elements) of a site with C channels: 80-byte rows
+// for 32 channels keep the 8 rows of an ldmatrix in distinct banks
+template <int C> struct Row { static constexpr int S = C == 32 ? 40 : 8; };
+
+// Stage the (TZ=1) x TY x TX tile's halo of a channels-last lattice
+// [nz][ny][nx][C] into shared memory rows of Row<C>::S elements.
+template <int C>
+__device__ __forceinline__ void load_halo(__nv_bfloat16* sm, const __nv_bfloat16* src, int nx, int ny, int nz,
+                                          int x0, int y0, int z0) {
+  constexpr int CH = C / 8;  // 16-byte chunks per site
+  for (int i = threadIdx.x; i < HSITES * CH; i += blockDim.x) {
+    const int s = i / CH, c = i % CH;
+    const int hx = s % HX, hy = (s / HX) % HY, hz = s / (HX * HY);
+    int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
+    x = x < 0 ? x + nx : (x >= nx ? x - nx : x);
+    y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+    z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+    const int64_t g = (((int64_t)z * ny + y) * nx + x) * C + c * 8;
+    cp16(sm + s * Row<C>::S + c * 8, src + g);
+  }
+}
+
+// ---------------------------------------------------------------- conv
+// out[s][n] = epi( sum_tap sum_k in[s + off(tap)][k] * W[tap][n][k] )
+// EPI_GELU:   z = acc + b; zout = z (optional); out = gelu(z)        (BF16)
+// EPI_LINEAR: out = acc + b, first two channels, FP32 [s][2]
+// EPI_BWD:    out = acc * gelu'(zin[s][n])                            (BF16)
+template <int CA, int CB, int EPI, bool STORE_Z>
+__global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
+  constexpr int SA = Row<CA>::S, SW = Row<CA>::S;
+  constexpr int NT = CB / 8;  // n-tiles of 8 output channels
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __nv_bfloat16* wsm = reinterpret_cast<__nv_bfloat16*>(smraw);  // [27][CB][SW]
+  __nv_bfloat16* hsm = wsm + 27 * CB * SW;                        // [HSITES][SA]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t4 = lane & 3;
+  // weights once per block
+  {
+    constexpr int CH = CA / 8;
+    const __nv_bfloat16* W = a.w;
+    for (int i = tid; i < 27 * CB * CH; i += blockDim.x) {
+      const int row = i / CH, c = i % CH;
+      cp16(wsm + row * SW + c * 8, W + (int64_t)row * CA + c * 8);
+    }
+    cp_commit();
+  }
+  float bias[NT][2];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) {
+    bias[nt][0] = a.bias ? a.bias[nt * 8 + 2 * t4] : 0.f;
+    bias[nt][1] = a.bias ? a.bias[nt * 8 + 2 * t4 + 1] : 0.f;
+  }
+  const int tiles_x = a.nx / TX, tiles_y = a.ny / TY;
+  const int64_t tiles_per = (int64_t)tiles_x * tiles_y * a.nz;
+  const int64_t ntiles = tiles_per * a.nlat;
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t lat_i = tile / tiles_per;
+    int64_t r = tile % tiles_per;
+    const int tx = (int)(r % tiles_x);
+    r /= tiles_x;
+    const int ty = (int)(r % tiles_y);
+    const int z0 = (int)(r / tiles_y);
+    const int x0 = tx * TX, y0 = ty * TY;
+    const __nv_bfloat16* src = a.in + lat_i * Nsite * CA;
+    __syncthreads();  // previous tile's reads of the halo are done
+    load_halo<CA>(hsm, src, a.nx, a.ny, a.nz, x0, y0, z0);
+    cp_commit();
+    cp_wait_all();
+    __syncthreads();
+
+    float acc[2][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
+
+#pragma unroll 1
+    for (int tap = 0; tap < 27; ++tap) {
+      const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // halo offsets 0..2
+      const __nv_bfloat16* wt = wsm + tap * CB * SW;
+      if constexpr (CA == 32) {
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) {
+          // B fragments for all n-tiles of this k-step
+          uint32_t b[NT][2];
+          if constexpr (NT >= 2) {
+#pragma unroll
+            for (int np = 0; np < NT / 2; ++np) {
+              const int idx = lane >> 3, rr = lane & 7;
+              const int n = np * 16 + rr + 8 * (idx >> 1), k = kk * 16 + 8 * (idx & 1);
+              uint32_t q[4];
+              ldsm_x4(q, wt + n * SW + k);
+              b[2 * np][0] = q[0]; b[2 * np][1] = q[1];
+              b[2 * np + 1][0] = q[2]; b[2 * np + 1][1] = q[3];
+            }
+          } else {
+            const int idx = (lane >> 3) & 1, rr = lane & 7;
+            uint32_t q[2];
+            ldsm_x2(q, wt + rr * SW + kk * 16 + 8 * idx);
+            b[0][0] = q[0]; b[0][1] = q[1];
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
+            const int yy = 2 * warp + mt;  // tile row of this m-tile
+            const int idx = lane >> 3, rr = lane & 7;
+            const int xs = rr + 8 * (idx & 1);
+            const int hs = (dz * HY + (yy + dy)) * HX + (xs + dx);
+            uint32_t af[4];
+            ldsm_x4(af, hsm + hs * SA + kk * 16 + 8 * (idx >> 1));
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt) mma16816(acc[mt][nt], af, b[nt][0], b[nt][1]);
+          }
+        }
+      } else {  // CA == 8: one k8 step per tap
+        uint32_t b[NT];
+        if constexpr (NT == 4) {
+          const int idx = lane >> 3, rr = lane & 7;
+          uint32_t q[4];
+          ldsm_x4(q, wt + (idx * 8 + rr) * SW);
+          b[0] = q[0]; b[1] = q[1]; b[2] = q[2]; b[3] = q[3];
+        } else {
+          ldsm_x1(b[0], wt + (lane & 7) * SW);
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+          const int yy = 2 * warp + mt;
+          const int xs = (lane & 7) + 8 * ((lane >> 3) & 1);
+          const int hs = (dz * HY + (yy + dy)) * HX + (xs + dx);
+          uint32_t af[2];
+          ldsm_x2(af, hsm + hs * SA);
+#pragma unroll
+          for (int nt = 0; nt < NT; ++nt) mma1688(acc[mt][nt], af, b[nt]);
+        }
+      }
+    }
+    // epilogue: rows g and g+8 of each m-tile are x = g, g + 8
+    const int64_t obase = lat_i * Nsite;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const int y = y0 + 2 * warp + mt;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int x = x0 + g + 8 * h;
+        const int64_t s = obase + ((int64_t)z0 * a.ny + y) * a.nx + x;
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const int n = nt * 8 + 2 * t4;
+          float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
+          if constexpr (EPI == EPI_GELU) {
+            v0 += bias[nt][0];
+            v1 += bias[nt][1];
+            if constexpr (STORE_Z)
+              *reinterpret_cast<__nv_bfloat162*>(a.zout + s * CB + n) = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162*>(a.out + s * CB + n) = __floats2bfloat162_rn(gelu(v0), gelu(v1));
+          } else if constexpr (EPI == EPI_LINEAR) {
+            if (nt == 0 && t4 == 0)
+              *reinterpret_cast<float2*>(a.outf + s * 2) = make_float2(v0 + bias[0][0], v1 + bias[0][1]);
+          } else {
+            const __nv_bfloat162 zz = *reinterpret_cast<const __nv_bfloat162*>(a.zin + s * CB + n);
+            const float z0f = __bfloat162float(zz.x), z1f = __bfloat162float(zz.y);
+            *reinterpret_cast<__nv_bfloat162*>(a.out + s * CB + n) =
+                __floats2bfloat162_rn(v0 * gelu_d(z0f), v1 * gelu_d(z1f));
+          }
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- weight gradient
+// part[blk][tap][i][o] = sum over the block's sites s of X[s + off(tap)][i] * D[s][o]
+// (X: CX channels, halo-shifted; D: CD channels).  The GEMM's M side is the
+// 32-channel operand.  part_b[blk][o] = sum_s D[s][o].
+template <int CX, int CD>
+__global__ void __launch_bounds__(288) wgrad_kernel(WgradArgs a) {
+  constexpr bool MX = CX == 32;  // M = X channels (else M = D channels)
+  constexpr int CN = MX ? CD : CX;
+  constexpr int NT = CN / 8;
+  constexpr int SX = Row<CX>::S, SD = Row<CD>::S;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __nv_bfloat16* xs = reinterpret_cast<__nv_bfloat16*>(smraw);  // [HSITES][SX]
+  __nv_bfloat16* ds = xs + HSITES * SX;                           // [TSITES][SD]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;  // 9 warps
+  const int g = lane >> 2, t4 = lane & 3;
+  float acc[3][2][NT][4];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[j][mt][nt][q] = 0.f;
+  float bsum = 0.f;  // thread tid < CD: channel tid of D
+
+  const int tiles_x = a.nx / TX, tiles_y = a.ny / TY;
+  const int64_t tiles_per = (int64_t)tiles_x * tiles_y * a.nz;
+  const int64_t ntiles = tiles_per * a.nlat;
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t lat_i = tile / tiles_per;
+    int64_t r = tile % tiles_per;
+    const int tx = (int)(r % tiles_x);
+    r /= tiles_x;
+    const int ty = (int)(r % tiles_y);
+    const int z0 = (int)(r / tiles_y);
+    const int x0 = tx * TX, y0 = ty * TY;
+    __syncthreads();
+    load_halo<CX>(xs, a.x + lat_i * Nsite * CX, a.nx, a.ny, a.nz, x0, y0, z0);
+    {
+      constexpr int CH = CD / 8;
+      const __nv_bfloat16* D = a.d + lat_i * Nsite * CD;
+      for (int i = tid; i < TSITES * CH; i += blockDim.x) {
+        const int s = i / CH, c = i % CH;
+        const int xx = s % TX, yy = s / TX;
+        cp16(ds + s * SD + c * 8, D + (((int64_t)z0 * a.ny + y0 + yy) * a.nx + x0 + xx) * CD + c * 8);
+      }
+    }
+    cp_commit();
+    cp_wait_all();
+    __syncthreads();
+    if (tid < CD)
+      for (int s = 0; s < TSITES; ++s) bsum += __bfloat162float(ds[s * SD + tid]);
+
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int tap = warp + 9 * j;
+      const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll 1
+      for (int ky = 0; ky < TY; ++ky) {  // 16 sites of tile row ky per k-step
+        // shifted X rows: halo site of tile site (xx, ky) moved by the tap
+        auto xrow = [&](int xx) { return ((dz * HY) + (ky + dy)) * HX + (xx + dx); };
+        auto drow = [&](int xx) { return ky * TX + xx; };
+        const int idx = lane >> 3, rr = lane & 7;
+        // M operand (2 m-tiles of 16 channels): ldmatrix.trans of [site][chan]
+        uint32_t am[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+          const int site = rr + 8 * (idx >> 1), ch = mt * 16 + 8 * (idx & 1);
+          if constexpr (MX) ldsm_x4_t(am[mt], xs + xrow(site) * SX + ch);
+          else ldsm_x4_t(am[mt], ds + drow(site) * SD + ch);
+        }
+        // N operand (NT n-tiles of 8 channels)
+        uint32_t bn[NT][2];
+        if constexpr (NT >= 2) {
+#pragma unroll
+          for (int np = 0; np < NT / 2; ++np) {
+            const int site = rr + 8 * (idx & 1), ch = np * 16 + 8 * (idx >> 1);
+            uint32_t q[4];
+            if constexpr (MX) ldsm_x4_t(q, ds + drow(site) * SD + ch);
+            else ldsm_x4_t(q, xs + xrow(site) * SX + ch);
+            bn[2 * np][0] = q[0]; bn[2 * np][1] = q[1];
+            bn[2 * np + 1][0] = q[2]; bn[2 * np + 1][1] = q[3];
+          }
+        } else {
+          const int site = rr + 8 * (idx & 1);
+          uint32_t q[2];
+          if constexpr (MX) ldsm_x2_t(q, ds + drow(site) * SD);
+          else ldsm_x2_t(q, xs + xrow(site) * SX);
+          bn[0][0] = q[0]; bn[0][1] = q[1];
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < NT; ++nt) mma16816(acc[j][mt][nt], am[mt], bn[nt][0], bn[nt][1]);
+      }
+    }
+  }
+  // partials in [tap][x-chan][d-chan] order
+  float* part = a.part + (int64_t)blockIdx.x * 27 * CX * CD;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const int tap = warp + 9 * j;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int m = mt * 16 + g + 8 * (q >> 1), n = nt * 8 + 2 * t4 + (q & 1);
+          const int i = MX ? m : n, o = MX ? n : m;
+          part[(tap * CX + i) * CD + o] = acc[j][mt][nt][q];
+        }
+  }
+  if (tid < CD) a.part_b[(int64_t)blockIdx.x * CD + tid] = bsum;
+}
+
+// grad[e] = sum over blocks of part[blk][e], blocks in index order
+__global__ void reduce_parts_kernel(const float* __restrict__ part, int nblk, int64_t per, float* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < per; e += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * per + e];
+    out[e] = s;
+  }
+}
+
+// ------------------------------------------------------------ pointwise
+// channels-last BF16 input [lat][site][8] from four FP32/FP64 channel arrays,
+// normalised: (x - shift) * scale; channels 4..7 are zero
+template <typename R>
+__global__ void pack_kernel(PackArgs a) {
+  const int64_t total = a.nlat * a.N;
+  double u[4] = {1.0, 1.0, 1.0, 1.0};
+  if (a.sc) {
+    const double av = __ldcg(&a.sc->a);
+    u[0] = u[1] = av;
+    u[2] = u[3] = 1.0 / av;
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = i / a.N, s = i % a.N;
+    const int64_t base = a.idx ? (int64_t)a.idx[l] * a.lat_stride : l * a.lat_stride;
+    __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const R* p = static_cast<const R*>(a.ch[c]);
+      const float x = (float)(((double)p[base + s] * u[c] - a.shift[c]) * a.scale[c]);
+      v[c] = __float2bfloat16_rn(x);
+    }
+#pragma unroll
+    for (int c = 4; c < 8; ++c) v[c] = __float2bfloat16_rn(0.f);
+    *reinterpret_cast<uint4*>(a.out + i * 8) = *reinterpret_cast<const uint4*>(v);
+  }
+}
+
+// MSE against the scaled targets; dout = 2 (out - t) / count in BF16 [site][8]
+__global__ void loss_kernel(LossArgs a) {
+  const int64_t total = a.nlat * a.N;
+  double local = 0.0;
+  const double inv = 1.0 / (2.0 * (double)total);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = i / a.N, s = i % a.N;
+    const int64_t base = (int64_t)a.idx[l] * a.lat_stride;
+    const float2 o = *reinterpret_cast<const float2*>(a.out + i * 2);
+    const float t0 = (float)(a.t0[base + s] * a.tscale[0]), t1 = (float)(a.t1[base + s] * a.tscale[1]);
+    const float e0 = o.x - t0, e1 = o.y - t1;
+    local += (double)e0 * e0 + (double)e1 * e1;
+    __align__(16) __nv_bfloat16 v[8];
+    v[0] = __float2bfloat16_rn((float)(2.0 * inv) * e0);
+    v[1] = __float2bfloat16_rn((float)(2.0 * inv) * e1);
+#pragma unroll
+    for (int c = 2; c < 8; ++c) v[c] = __float2bfloat16_rn(0.f);
+    *reinterpret_cast<uint4*>(a.dout + i * 8) = *reinterpret_cast<const uint4*>(v);
+  }
+  // block sum into part[blockIdx]
+  __shared__ double ws[32];
+  local = warp_sum(local);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = v * inv;
+  }
+}
+
+__global__ void sum_kernel(const double* __restrict__ part, int n, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += part[i];
+    *out = s;
+  }
+}
+
+// Adam step on the flat FP32 parameters (bias-corrected)
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                            float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float g = gr[i];
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// BF16 copies of one layer's weights W[tap][i][o] (FP32):
+//   fwd[tap][o][i] = W[tap][i][o];   bwd[tap][i][o] = W[26 - tap][i][o]
+__global__ void repack_kernel(const float* __restrict__ W, int ci, int co, __nv_bfloat16* __restrict__ fwd,
+                              __nv_bfloat16* __restrict__ bwd) {
+  const int n = 27 * ci * co;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int tap = e / (ci * co), r = e % (ci * co), i = r / co, o = r % co;
+    fwd[(tap * co + o) * ci + i] = __float2bfloat16_rn(W[e]);
+    if (bwd) bwd[((26 - tap) * ci + i) * co + o] = __float2bfloat16_rn(W[e]);
+  }
+}
+
+// closure kick: pi_f += hk a^4 Delta_f with Delta_f = out[s][f] / tscale[f] (units 0) or
+// a^3 Delta_f = out[s][f] / tscale[f] (units 1); a = 1 in Minkowski
+template <typename R>
+__global__ void corr_kick_kernel(CorrArgs a) {
+  double av = 1.0;
+  if (a.conf) av = __ldcg(&a.sc->a);
+  const double f = a.units ? av : av * av * av * av;  // a^4 Delta = a (a^3 Delta)
+  const R c0 = (R)(a.hk * f / a.tscale[0]), c1 = (R)(a.hk * f / a.tscale[1]);
+  R* p0 = static_cast<R*>(a.pi);
+  R* p1 = p0 + a.N;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.N; s += (int64_t)gridDim.x * blockDim.x) {
+    const float2 o = *reinterpret_cast<const float2*>(a.out + s * 2);
+    p0[s] += c0 * (R)o.x;
+    p1[s] += c1 * (R)o.y;
+  }
+}
+
+template <int CA, int CB, int EPI, bool SZ>
+int conv_go(const ConvArgs& a, int nsm, cudaStream_t s) {
+  constexpr size_t smem = (size_t)(27 * CB * Row<CA>::S + HSITES * Row<CA>::S) * 2;
+  auto k = conv_kernel<CA, CB, EPI, SZ>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_fail(e, "conv smem attribute");
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, smem);
+  if (per_sm < 1) per_sm = 1;
+  const int64_t ntiles = (int64_t)(a.nx / TX) * (a.ny / TY) * a.nz * a.nlat;
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)nsm * per_sm);
+  k<<<(unsigned)grid, 128, smem, s>>>(a);
+  if (g_launch_counter) ++*g_launch_counter;
+  e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "conv launch");
+}
+
+}  // namespace
+
+int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s) {
+  if (a.nx % TX || a.ny % TY || a.nz < 1) return set_error(LAT_ERR_ARG, "closure lattice: nx % 16, ny % 8");
+  const bool sz = a.zout != nullptr;
+  if (ca == 8 && cb == 32 && epi == EPI_GELU) return sz ? conv_go<8, 32, EPI_GELU, true>(a, nsm, s)
+                                                        : conv_go<8, 32, EPI_GELU, false>(a, nsm, s);
+  if (ca == 32 && cb == 32 && epi == EPI_GELU) return sz ? conv_go<32, 32, EPI_GELU, true>(a, nsm, s)
+                                                         : conv_go<32, 32, EPI_GELU, false>(a, nsm, s);
+  if (ca == 32 && cb == 8 && epi == EPI_LINEAR) return conv_go<32, 8, EPI_LINEAR, false>(a, nsm, s);
+  if (ca == 8 && cb == 32 && epi == EPI_BWD) return conv_go<8, 32, EPI_BWD, false>(a, nsm, s);
+  if (ca == 32 && cb == 32 && epi == EPI_BWD) return conv_go<32, 32, EPI_BWD, false>(a, nsm, s);
+  return set_error(LAT_ERR_UNSUPPORTED, "conv shape");
+}
+
+int wgrad_blocks(int nsm) { return nsm; }
+
+int wgrad(const WgradArgs& a, int cx, int cd, int nblk, float* dW, float* db, cudaStream_t s) {
+  if (a.nx % TX || a.ny % TY) return set_error(LAT_ERR_ARG, "closure lattice: nx % 16, ny % 8");
+  size_t smem = 0;
+  cudaError_t e;
+  auto go = [&](auto kern, int CX, int CD) -> int {
+    smem = (size_t)(HSITES * (CX == 32 ? 40 : 8) + TSITES * (CD == 32 ? 40 : 8)) * 2;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "wgrad smem attribute");
+    kern<<<nblk, 288, smem, s>>>(a);
+    if (g_launch_counter) ++*g_launch_counter;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? LAT_OK : cuda_fail(e, "wgrad launch");
+  };
+  int st;
+  if (cx == 32 && cd == 8) st = go(wgrad_kernel<32, 8>, 32, 8);
+  else if (cx == 32 && cd == 32) st = go(wgrad_kernel<32, 32>, 32, 32);
+  else if (cx == 8 && cd == 32) st = go(wgrad_kernel<8, 32>, 8, 32);
+  else return set_error(LAT_ERR_UNSUPPORTED, "wgrad shape");
+  if (st != LAT_OK) return st;
+  const int64_t per = 27LL * cx * cd;
+  reduce_parts_kernel<<<(unsigned)((per + 255) / 256), 256, 0, s>>>(a.part, nblk, per, dW);
+  reduce_parts_kernel<<<1, 256, 0, s>>>(a.part_b, nblk, cd, db);
+  if (g_launch_counter) *g_launch_counter += 2;
+  e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "wgrad reduce launch");
+}
+
+int pack(const PackArgs& a, int fp64, int nsm, cudaStream_t s) {
+  const int64_t total = a.nlat * a.N;
+  const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)nsm * 8);
+  if (fp64) pack_kernel<double><<<grid, 256, 0, s>>>(a);
+  else pack_kernel<float><<<grid, 256, 0, s>>>(a);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "pack launch");
+}
+
+int loss(const LossArgs& a, int nblk, double* out, cudaStream_t s) {
+  loss_kernel<<<nblk, 256, 0, s>>>(a);
+  sum_kernel<<<1, 32, 0, s>>>(a.part, nblk, out);
+  if (g_launch_counter) *g_launch_counter += 2;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "loss launch");
+}
+
+int adam(float* p, const float* g, float* m, float* v, int64_t n, double lr, int64_t step, cudaStream_t s) {
+  const double b1 = 0.9, b2 = 0.999;
+  const float c1 = (float)(1.0 - pow(b1, (double)step)), c2 = (float)(1.0 - pow(b2, (double)step));
+  adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, g, m, v, n, (float)lr, (float)b1, (float)b2, 1e-8f, c1,
+                                                           c2);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "adam launch");
+}
+
+int repack(const float* W, int ci, int co, __nv_bfloat16* fwd, __nv_bfloat16* bwd, cudaStream_t s) {
+  repack_kernel<<<(27 * ci * co + 255) / 256, 256, 0, s>>>(W, ci, co, fwd, bwd);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "repack launch");
+}
+
+int corr_kick(const CorrArgs& a, int fp64, int nsm, cudaStream_t s) {
+  const unsigned grid = (unsigned)std::min<int64_t>((a.N + 255) / 256, (int64_t)nsm * 8);
+  if (fp64) corr_kick_kernel<double><<<grid, 256, 0, s>>>(a);
+  else corr_kick_kernel<float><<<grid, 256, 0, s>>>(a);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "closure kick launch");
+}
+
+}  // namespace net
+}  // namespace lat

@@ -298,3 +298,31 @@ def test_graph_replay_matches_eager(engine, monkeypatch):
         g.symp(2, 0.03, 3)
     b = g.get_state()
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_prepared_graph_leaves_state_and_replays(engine):
+    """lat_symp_prepare captures without running: state, scale factor and time
+    are unchanged, and the next symp call replays the prepared graph."""
+    c = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                      precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0),
+                      spectral_impl=L.SPEC_IMPL_SEPARABLE)
+    f, p = random_state((2, 32, 32, 64), seed=12)
+    out = []
+    for prepare in (False, True):
+        g = engine.Lattice(c)
+        g.set_state(f, p)
+        g.set_scale_factor(1.0, 0.0)
+        g.calc_metric()
+        before = g.get_state(), g.scale_factor(), g.time()
+        if prepare:
+            g.prepare_symp(4, 0.01, 3)
+            assert np.array_equal(g.get_state()[0], before[0][0])
+            assert g.scale_factor() == before[1] and list(g.time()) == list(before[2])
+            l0 = g.launch_count()
+        g.symp(4, 0.01, 3)
+        if prepare:
+            assert g.launch_count() > l0
+        out.append((g.get_state(), g.scale_factor()))
+        g.close()
+    assert np.array_equal(out[0][0][0], out[1][0][0]) and np.array_equal(out[0][0][1], out[1][0][1])
+    assert out[0][1] == out[1][1]

@@ -27,7 +27,9 @@ def _lattice(engine, cfg, separable=True):
     return g
 
 
-@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 32, 16), (16, 64, 128)])
+# (nx, ny, nz): the y and z passes cover whole blocks of x-columns, so nx is a
+# multiple of the pass's column block (64 or 128 columns for short lines)
+@pytest.mark.parametrize("shape", [(128, 32, 32), (128, 64, 16), (256, 16, 64)])
 @pytest.mark.parametrize("nf", [1, 2])
 @pytest.mark.parametrize("conf", [False, True])
 @pytest.mark.parametrize("prec", [L.FP64, L.FP32_KAHAN])
@@ -102,11 +104,11 @@ def test_autotune_preserves_state_and_caches(engine, tmp_path, kind):
     if kind == "fd":
         c = L.make_config(32, nfld=1, length=8.0, laplacian=L.LAP_FD27, precision=L.FP32_KAHAN,
                           model=L.MODEL_DOUBLE_WELL, model_params=(0.01,), gw=True, gw_coupling=2.0)
-    else:
-        c = L.make_config(32, nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+    else:  # 64 x 32 x 32 admits the separable passes, so the tuner times both spectral paths
+        c = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
                           precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
     g = engine.Lattice(c)
-    f, p = random_state((c.nfld, 32, 32, 32), seed=5)
+    f, p = random_state((c.nfld, c.nz, c.ny, c.nx), seed=5)
     g.set_state(f, p)
     g.set_scale_factor(1.1, -0.3)
     before = g.get_state(), g.scale_factor()
@@ -130,4 +132,18 @@ def test_autotune_preserves_state_and_caches(engine, tmp_path, kind):
         obj.set_state(f, p)
         obj.set_scale_factor(1.1, -0.3)
         obj.symp(2, 0.01, 4)
-    assert rel_err(g.get_state()[0], u.get_state()[0]) <= 1e-6
+    assert rel_err(g.get_state()[0], u.get_state()[0]) <= 5e-6
+
+
+def test_separable_unsupported_sizes_refused(engine):
+    """A separable request the passes cannot tile is refused at creation
+    (nothing falls back silently); AUTO on the same size keeps cuFFT."""
+    c = L.make_config(32, nfld=1, length=16.0, laplacian=L.LAP_SPECTRAL, spectral_impl=L.SPEC_IMPL_SEPARABLE)
+    with pytest.raises(engine.LatticeError) as ei:
+        engine.Lattice(c)
+    assert ei.value.code == 8  # LAT_ERR_UNSUPPORTED
+    c.spectral_impl = L.SPEC_IMPL_AUTO
+    g = engine.Lattice(c)
+    g.autotune()
+    assert g.tuning()[5] == L.SPEC_IMPL_CUFFT
+    g.close()
