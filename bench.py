@@ -221,6 +221,8 @@ def run_ours(args):
         return run_fd_case(L, args, local)
     if args.case == "closure":
         return run_closure_case(L, args, local)
+    if args.case == "ensemble":
+        return run_ensemble_case(L, args)
     n = args.n or N_SIDE
     impl = {"auto": L.SPEC_IMPL_AUTO, "cufft": L.SPEC_IMPL_CUFFT, "separable": L.SPEC_IMPL_SEPARABLE}[args.spectral_impl]
     c = workload_config(L, L.FP32_KAHAN, n, impl)
@@ -423,9 +425,10 @@ def diagnostics(L, g, args, dt, ms_step):
                   "steps_per_call": sub, "calls": reps,
                   "call": f"lat_upload + lat_symp(4, dt, {sub}) + lat_energies + lat_download "
                           "(FP64 Fortran-layout pinned host arrays, host clock around the calls)"}
-    # ---- the other workloads of the engine (FD stencil paths)
+    # ---- the other workloads of the engine (FD stencil paths, batched ensemble)
     if not args.no_fd:
         out["fd_workloads"] = fd_workloads(L, hbm)
+        out["ensemble"] = ensemble_workload(L, 100)
     # ---- CPU restatement on the host cores
     if not args.no_cpu:
         rate, cores, done, el = cpu_rate(steps_budget_s=args.cpu_budget, max_steps=args.cpu_steps)
@@ -433,6 +436,41 @@ def diagnostics(L, g, args, dt, ms_step):
                                "sample": f"{done} Yoshida-4 steps of the same 256^3 workload in FP64 "
                                          f"({el:.1f} s) after 1 warm-up step; CPU restatement of the "
                                          "Fortran reference, OpenMP"}
+    return out
+
+
+ENSEMBLE_SIZES = [64] * 32 + [96] * 32 + [128] * 24 + [192] * 8
+
+
+def ensemble_workload(L, steps, warmup=3, tune=True):
+    """96 independent phi^4 runs of uneven sizes (32 x 64^3, 32 x 96^3, 24 x 128^3,
+    8 x 192^3), L = 20, spectral, Yoshida-4, dt = dx/20, FP32-Kahan, advanced
+    together by one persistent pass per kick and a CUDA graph per call."""
+    base = L.make_config(64, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=L.FP32_KAHAN,
+                         model=L.MODEL_PHI4, model_params=(1.0,))
+    ens = L.Ensemble(base, ENSEMBLE_SIZES)
+    seeds = list(range(5000, 5000 + len(ENSEMBLE_SIZES)))
+    ens.init_vacuum(seeds, 1.0, 0.0, 3.0, amp=1e-8, kcut_frac=0.5)
+    if tune:
+        ens.autotune(os.environ.get("LAT_TUNE_CACHE"))
+    dto = 1.0 / 20
+    ens.symp(4, dto, warmup)
+    ens.prepare_symp(4, dto, steps)
+    ens.sync()
+    l0 = ens.launch_count()
+    ens.mark(0)
+    ens.symp(4, dto, steps)
+    ens.mark(1)
+    ms = ens.mark_elapsed(0, 1)
+    launches = ens.launch_count() - l0
+    E = ens.energies()
+    S, W = ens.spectrum(len(ENSEMBLE_SIZES) - 1, 64)
+    sites = sum(n ** 3 for n in ENSEMBLE_SIZES)
+    out = {"runs": len(ENSEMBLE_SIZES), "sizes": "32x64^3 + 32x96^3 + 24x128^3 + 8x192^3", "steps": steps,
+           "ms_per_step": ms / steps, "runs_per_s_1000_steps": len(ENSEMBLE_SIZES) / (ms / steps * 1000 * 1e-3),
+           "site_updates_per_s": sites * steps / (ms * 1e-3), "tuning": ens.tuning(), "gpu_launches": launches,
+           "energy_finite": bool(np.all(np.isfinite(E))), "spectrum_bins_nonzero": int(np.count_nonzero(W))}
+    ens.close()
     return out
 
 
@@ -497,6 +535,14 @@ def init_bubbles(g, n):
     ln = n / 4.0
     g.init_bubbles([[0.34375 * ln, 0.5 * ln, 0.5 * ln], [0.65625 * ln, 0.5 * ln, 0.5 * ln]], 0.09375 * ln,
                    math.sqrt(2.0))
+
+
+def run_ensemble_case(L, args):
+    """The batched uneven-size ensemble alone: 96 runs x --steps Yoshida-4 steps."""
+    res = ensemble_workload(L, args.steps, args.warmup)
+    print(json.dumps({"metric": "ensemble runs/s (96 uneven runs of 1000 Yoshida-4 steps, FP32-Kahan)",
+                      "value": res["runs_per_s_1000_steps"], "unit": "runs/s", "case": "ensemble", **res}))
+    return 0
 
 
 def run_fd_case(L, args, local):
@@ -641,7 +687,7 @@ def main():
     ap.add_argument("--spectral-impl", default="auto", choices=["auto", "cufft", "separable"])
     ap.add_argument("--n", type=int, default=None,
                     help="lattice side: headline 256 (other sides for profiling), fd-bubbles 256, closure coarse 64")
-    ap.add_argument("--case", default="headline", choices=["headline", "fd-bubbles", "closure"],
+    ap.add_argument("--case", default="headline", choices=["headline", "fd-bubbles", "closure", "ensemble"],
                     help="fd-bubbles: the 27-point bubble-collision workload with GW sourcing at side --n; "
                          "closure: learned subgrid closure, fine --n-fine^3 filtered to --n^3")
     ap.add_argument("--n-fine", type=int, default=256)

@@ -274,6 +274,18 @@ int lat_ens_energies(lat_ens_t* e, double* out /* nruns x LAT_NENERGY */);
 int lat_ens_spectrum(lat_ens_t* e, int32_t run, int32_t nbins, double* S, double* W);
 int lat_ens_download(lat_ens_t* e, int32_t run, double* fld, double* fldp);
 int lat_ens_sync(lat_ens_t* e);
+/* Graph of lat_ens_symp(e, order, dt_over_dx, nsteps) built without running it. */
+int lat_ens_prepare(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps);
+/* CUDA events on the ensemble's stream (slots 0..15) and the device time between two. */
+int lat_ens_mark(lat_ens_t* e, int32_t slot);
+int lat_ens_mark_elapsed(lat_ens_t* e, int32_t slot_a, int32_t slot_b, double* ms);
+int lat_ens_launch_count(const lat_ens_t* e, int64_t* count);
+/* Times the persistent passes' block size and blocks per SM on this ensemble
+ * (state saved and restored), keeps the fastest and caches it in cache_path
+ * (JSON lines keyed by precision, SM count and the run sizes); NULL: no cache. */
+int lat_ens_autotune(lat_ens_t* e, const char* cache_path);
+/* out[0] threads per block, out[1] blocks per SM of the persistent passes */
+int lat_ens_tuning_get(const lat_ens_t* e, int32_t out[2]);
 
 /* ------------------------------------------------- learned subgrid closure */
 /* No reference counterpart.  A coarse lattice evolved with a kick corrected

@@ -110,7 +110,9 @@ def _declare(lib: C.CDLL) -> None:
         "lat_ens_destroy": ([P], I), "lat_ens_init_vacuum": ([P, C.POINTER(U64), D, D, D, D, D], I),
         "lat_ens_symp": ([P, I, D, I], I), "lat_ens_energies": ([P, dp], I),
         "lat_ens_spectrum": ([P, I, I, dp, dp], I), "lat_ens_download": ([P, I, dp, dp], I),
-        "lat_ens_sync": ([P], I),
+        "lat_ens_sync": ([P], I), "lat_ens_prepare": ([P, I, D, I], I), "lat_ens_mark": ([P, I], I),
+        "lat_ens_mark_elapsed": ([P, I, I, dp], I), "lat_ens_launch_count": ([P, C.POINTER(I64)], I),
+        "lat_ens_autotune": ([P, C.c_char_p], I), "lat_ens_tuning_get": ([P, C.POINTER(I)], I),
         "lat_timing_enable": ([P, I], I), "lat_timing_read": ([P, I, dp, C.POINTER(I64)], I),
         "lat_timing_reset": ([P], I), "lat_mark": ([P, I], I), "lat_mark_elapsed": ([P, I, I, dp], I), "lat_launch_count": ([P, C.POINTER(I64)], I),
         "lat_device_ptr": ([P, I, C.POINTER(P)], I), "lat_host_alloc": ([C.POINTER(P), C.c_size_t], I),
@@ -545,6 +547,30 @@ class Ensemble:
 
     def sync(self):
         _check(_lib.lat_ens_sync(self._h))
+
+    def prepare_symp(self, order, dt_over_dx, nsteps):
+        _check(_lib.lat_ens_prepare(self._h, order, dt_over_dx, nsteps))
+
+    def mark(self, slot):
+        _check(_lib.lat_ens_mark(self._h, slot))
+
+    def mark_elapsed(self, a, b) -> float:
+        ms = C.c_double()
+        _check(_lib.lat_ens_mark_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        _check(_lib.lat_ens_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def autotune(self, cache_path=None):
+        _check(_lib.lat_ens_autotune(self._h, None if cache_path is None else str(cache_path).encode()))
+
+    def tuning(self):
+        out = (C.c_int32 * 2)()
+        _check(_lib.lat_ens_tuning_get(self._h, out))
+        return list(out)
 
     def energies(self):
         out = np.zeros((len(self.sizes), NENERGY))

@@ -1553,7 +1553,7 @@ std::string tune_key(lat_s* h) {
   return buf;
 }
 
-bool tune_lookup(const char* path, const std::string& key, int v[4]) {
+bool tune_lookup(const char* path, const std::string& key, int v[5]) {
   if (!path) return false;
   FILE* fp = fopen(path, "r");
   if (!fp) return false;

@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -171,6 +173,7 @@ struct lat_ens_s {
   int grid = 0, block = 256;
   int64_t launches = 0;
   std::vector<EnsGraph> graphs;
+  cudaEvent_t marks[16] = {};
 };
 
 namespace {
@@ -352,6 +355,8 @@ int lat_ens_destroy(lat_ens_t* e) {
   if (!e) return LAT_OK;
   cudaSetDevice(e->dev);
   if (e->stream) cudaStreamSynchronize(e->stream);
+  for (auto& m : e->marks)
+    if (m) cudaEventDestroy(m);
   for (auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
   for (auto& c : e->cls)
     if (c.have) {
@@ -500,15 +505,146 @@ int lat_ens_init_vacuum(lat_ens_t* e, const uint64_t* seeds, double fld0, double
   return rc;
 }
 
+namespace {
+int ens_symp(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps, bool run);
+}
+
 int lat_ens_symp(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps) {
   if (!e) return set_error(LAT_ERR_ARG, "null handle");
   EGuard g(e);
+  return ens_symp(e, order, dt_over_dx, nsteps, true);
+}
+
+int lat_ens_prepare(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps) {
+  if (!e) return set_error(LAT_ERR_ARG, "null handle");
+  EGuard g(e);
+  return ens_symp(e, order, dt_over_dx, nsteps, false);
+}
+
+int lat_ens_mark(lat_ens_t* e, int32_t slot) {
+  if (!e || slot < 0 || slot >= 16) return set_error(LAT_ERR_ARG, "bad mark slot");
+  EGuard g(e);
+  if (!e->marks[slot]) ECK(cudaEventCreate(&e->marks[slot]));
+  ECK(cudaEventRecord(e->marks[slot], e->stream));
+  return LAT_OK;
+}
+
+int lat_ens_mark_elapsed(lat_ens_t* e, int32_t a, int32_t b, double* ms) {
+  if (!e || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !e->marks[a] || !e->marks[b])
+    return set_error(LAT_ERR_ARG, "bad mark slots");
+  EGuard g(e);
+  ECK(cudaEventSynchronize(e->marks[b]));
+  float t = 0;
+  ECK(cudaEventElapsedTime(&t, e->marks[a], e->marks[b]));
+  *ms = t;
+  return LAT_OK;
+}
+
+int lat_ens_launch_count(const lat_ens_t* e, int64_t* count) {
+  if (!e || !count) return set_error(LAT_ERR_ARG, "null argument");
+  *count = e->launches;
+  return LAT_OK;
+}
+
+int lat_ens_tuning_get(const lat_ens_t* e, int32_t out[2]) {
+  if (!e || !out) return set_error(LAT_ERR_ARG, "null argument");
+  out[0] = e->block;
+  out[1] = e->grid / e->nsm;
+  return LAT_OK;
+}
+
+int lat_ens_autotune(lat_ens_t* e, const char* cache_path) {
+  if (!e) return set_error(LAT_ERR_ARG, "null handle");
+  EGuard g(e);
+  std::string key = std::string("ens:") + (e->prec == LAT_FP64 ? "fp64" : "fp32k") + ":" + std::to_string(e->nsm);
+  for (size_t r = 0; r < e->run_cls.size(); ++r) key += ":" + std::to_string(e->cls[e->run_cls[r]].n);
+  if (cache_path) {  // a cached choice for this exact ensemble
+    FILE* fp = fopen(cache_path, "r");
+    if (fp) {
+      char line[4096];
+      const std::string pat = "\"key\": \"" + key + "\"";
+      int blk = 0, bps = 0;
+      bool found = false;
+      while (fgets(line, sizeof(line), fp)) {
+        if (!strstr(line, pat.c_str())) continue;
+        const char* q = strstr(line, "\"block\":");
+        if (q && sscanf(q, "\"block\": %d, \"bps\": %d", &blk, &bps) == 2) found = true;
+      }
+      fclose(fp);
+      if (found && blk > 0 && bps > 0) {
+        e->block = blk;
+        e->grid = e->nsm * bps;
+        for (auto& ge : e->graphs) cudaGraphExecDestroy(ge.exec);
+        e->graphs.clear();
+        return LAT_OK;
+      }
+    }
+  }
+  // candidates run real passes: save and restore the state
+  const size_t fb = (size_t)e->Ntot * e->rsz;
+  void* saved[3] = {nullptr, nullptr, nullptr};
+  void* live[3] = {e->phi, e->phic, e->pi};
+  for (int i = 0; i < 3; ++i)
+    if (live[i]) {
+      ECK(cudaMalloc(&saved[i], fb));
+      ECK(cudaMemcpyAsync(saved[i], live[i], fb, cudaMemcpyDeviceToDevice, e->stream));
+    }
+  std::vector<Op> ops;
+  double tg[3] = {0, 0, 0};
+  Emitter em{2, false, false, &ops, tg};
+  int st = em.symp(2, 1.0, 2);
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int bblk = e->block, bgrid = e->grid;
+  for (int blk : {128, 256})  // the persistent passes are built for at most 256 threads
+    for (int bps : {1, 2, 4, 8}) {
+      if (st != LAT_OK) break;
+      e->block = blk;
+      e->grid = e->nsm * bps;
+      st = ens_exec(e, ops, 1e-4);  // warm-up
+      cudaEventRecord(a, e->stream);
+      for (int r = 0; r < 3 && st == LAT_OK; ++r) st = ens_exec(e, ops, 1e-4);
+      cudaEventRecord(b, e->stream);
+      cudaEventSynchronize(b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (st == LAT_OK && ms < best) { best = ms; bblk = blk; bgrid = e->grid; }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e->block = bblk;
+  e->grid = bgrid;
+  for (int i = 0; i < 3; ++i)
+    if (saved[i]) cudaMemcpyAsync(live[i], saved[i], fb, cudaMemcpyDeviceToDevice, e->stream);
+  cudaStreamSynchronize(e->stream);
+  for (void* p : saved)
+    if (p) cudaFree(p);
+  for (auto& ge : e->graphs) cudaGraphExecDestroy(ge.exec);
+  e->graphs.clear();
+  if (st != LAT_OK) return st;
+  if (cache_path) {
+    FILE* fp = fopen(cache_path, "a");
+    if (fp) {
+      fprintf(fp, "{\"key\": \"%s\", \"block\": %d, \"bps\": %d}\n", key.c_str(), e->block, e->grid / e->nsm);
+      fclose(fp);
+    }
+  }
+  return LAT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int ens_symp(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps, bool run) {
   std::vector<Op> ops;
   double tg[3] = {0, 0, 0};
   Emitter em{2, false, false, &ops, tg};
   ERET(em.symp(order, 1.0, nsteps));  // unit step: every h scales with each class's dt
   for (auto& ge : e->graphs)
     if (ge.order == order && ge.dto == dt_over_dx && ge.nsteps == nsteps) {
+      if (!run) return LAT_OK;
       ECK(cudaGraphLaunch(ge.exec, e->stream));
       e->launches += ge.kernels;
       return LAT_OK;
@@ -533,9 +669,16 @@ int lat_ens_symp(lat_ens_t* e, int32_t order, double dt_over_dx, int32_t nsteps)
     e->graphs.erase(e->graphs.begin());
   }
   e->graphs.push_back(ge);
+  if (!run) {
+    e->launches = before;
+    return LAT_OK;
+  }
   ECK(cudaGraphLaunch(ge.exec, e->stream));
   return LAT_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int lat_ens_sync(lat_ens_t* e) {
   if (!e) return set_error(LAT_ERR_ARG, "null handle");

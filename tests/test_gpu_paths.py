@@ -147,3 +147,31 @@ def test_separable_unsupported_sizes_refused(engine):
     g.autotune()
     assert g.tuning()[5] == L.SPEC_IMPL_CUFFT
     g.close()
+
+
+def test_ensemble_autotune_preserves_state(engine, tmp_path):
+    base = L.make_config(16, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=L.FP32_KAHAN,
+                         model=L.MODEL_PHI4)
+    sizes = [16, 32, 16]
+    ens = engine.Ensemble(base, sizes)
+    ens.init_vacuum([1, 2, 3], 1.0, 0.0, 3.0, amp=1e-4, kcut_frac=0.5)
+    before = [ens.state(r) for r in range(3)]
+    cache = tmp_path / "ens.jsonl"
+    ens.autotune(cache)
+    after = [ens.state(r) for r in range(3)]
+    for b, a in zip(before, after):
+        assert np.array_equal(b[0], a[0]) and np.array_equal(b[1], a[1])
+    t = ens.tuning()
+    assert t[0] in (128, 256) and t[1] in (1, 2, 4, 8)
+    assert len(cache.read_text().splitlines()) == 1
+    other = engine.Ensemble(base, sizes)
+    other.autotune(cache)  # reuses the cached choice
+    assert other.tuning() == t and len(cache.read_text().splitlines()) == 1
+    # the tuned ensemble still evolves like an untuned one
+    other.init_vacuum([1, 2, 3], 1.0, 0.0, 3.0, amp=1e-4, kcut_frac=0.5)
+    fresh = engine.Ensemble(base, sizes)
+    fresh.init_vacuum([1, 2, 3], 1.0, 0.0, 3.0, amp=1e-4, kcut_frac=0.5)
+    for e in (other, fresh):
+        e.symp(4, 1.0 / 20, 5)
+    for r in range(3):
+        assert rel_err(other.state(r)[0], fresh.state(r)[0]) <= 1e-6
