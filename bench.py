@@ -607,7 +607,8 @@ def conv_roofline(L, net, n, reps=10):
     ach = N * sum(v[0] for v in CONV_FLOPS_PER_SITE.values()) / tot / 1e12
     out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                        "peak_kind": kind + " dense bf16 (cuBLAS burst)",
-                       "note": "mma.sync m16n8k16/m16n8k8 BF16 implicit-GEMM convolutions, FP32 accumulate"}
+                       "note": "conv2 (32->32) on tcgen05.mma with TMEM accumulators when nx % 128 == 0, "
+                               "conv1 and conv3 on mma.sync; BF16 in, FP32 accumulate"}
     return out
 
 

@@ -1138,6 +1138,11 @@ int lat_sync(lat_t* h) {
   unsigned int err = 0;
   CK(cudaMemcpy(&err, &h->sc->err, sizeof(unsigned int), cudaMemcpyDeviceToHost));
   if (err & 1u) return set_error(LAT_ERR_NAN, "NaN/Inf in a lattice reduction");
+  if (h->cl_net) {
+    int cerr = 0;
+    CK(cudaMemcpy(&cerr, net::net_err(h->cl_net), sizeof(int), cudaMemcpyDeviceToHost));
+    if (cerr) return set_error(LAT_ERR_TIMEOUT, "closure convolution: a tensor-core wait gave up");
+  }
   return LAT_OK;
 }
 

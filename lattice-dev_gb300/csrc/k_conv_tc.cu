@@ -1,0 +1,339 @@
+// k_conv_tc.cu -- the closure's 32 -> 32 channel 3x3x3 convolution on the
+// 5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory).
+//
+// Work item: a column of 128 x-sites x 2 y-rows marching through ZC z-planes.
+// Output plane z needs input planes z-1, z, z+1; the block keeps a ring of
+// four halo planes [y 4][channel chunk 4][x 130][8 channels] in shared
+// memory, so each step loads one new plane (33 KB for 256 outputs).
+//
+// Per step, for each of the two rows: M = 128 sites, N = 32 output channels,
+// K = 27 taps x 32 input channels = 54 tcgen05.mma (M128 N32 K16, BF16 in,
+// FP32 out) issued by one thread.  Both operands come from shared memory
+// through matrix descriptors in the no-swizzle K-major layout (8-row x
+// 16-byte core matrices):
+//   A: the 128 rows of one tap are 128 consecutive x of one halo row (core
+//      matrices 128 B apart); the tap's x offset is a 16-byte shift;
+//   B: the weights [tap 27][channel chunk 4][out 32][8], staged once.
+// Accumulators are double-buffered in TMEM (2 x 64 columns): the MMAs of
+// step j run while eight warps read back step j-1 (tcgen05.ld; warp w owns
+// TMEM lanes 32 (w mod 4) .. and columns 16 (w / 4) ..) for the epilogue
+// (bias + GELU, or times GELU' for the backward data pass) and the next
+// plane's copies are in flight.
+//
+// Every wait is bounded: a warp that gives up raises a shared abort flag that
+// the whole block reads after its next barrier; the block then sets the error
+// word, waits (bounded) for its own MMAs, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "net.hpp"
+
+namespace lat {
+namespace net {
+
+namespace {
+
+constexpr int TCX = 128, TCR = 2, ZC = 16;         // item: 128 x-sites, 2 y-rows, up to ZC z-planes
+constexpr int HXT = TCX + 2, HYT = TCR + 2;        // halo extents of one plane
+constexpr int CM_BYTES = 128;                      // one core matrix: 8 rows x 16 bytes
+constexpr int A_CHUNK = HXT * 16;                  // bytes between channel chunks (K direction) of A
+constexpr int A_YROW = 4 * A_CHUNK;                // bytes per halo y-row, all 4 chunks
+constexpr int A_PLANE = HYT * A_YROW;              // 33 280 bytes per halo plane
+constexpr int NSLOT = 4;                           // ring of halo planes
+constexpr int B_CHUNK = 32 * 16;                   // bytes between channel chunks of B
+constexpr int B_TAP = 4 * B_CHUNK;                 // 2 KB per tap
+constexpr int B_BYTES = 27 * B_TAP;                // 55 296
+constexpr int A_BYTES = NSLOT * A_PLANE;           // 133 120
+constexpr int TMEM_COLS = 128;                     // 2 buffers x 2 rows x 32 fp32 columns
+constexpr int SMEM_TC = B_BYTES + A_BYTES + 64;    // + two mbarriers and the TMEM address
+constexpr int THREADS = 256;
+constexpr uint32_t kSpinLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp16(uint32_t saddr, const void* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr), "l"(g) : "memory");
+}
+
+// shared-memory matrix descriptor, no swizzle, K-major
+__device__ __forceinline__ uint64_t mdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of this tensor-core generation
+  return d;                // base offset 0, absolute LBO mode 0, layout SWIZZLE_NONE (0)
+}
+
+// instruction descriptor: kind::f16, A and B BF16, D FP32, both K-major, M = 128, N = 32
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(addr), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_df(float z) {
+  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// copies of halo plane z (periodic) of an item into ring slot `slot`
+__device__ __forceinline__ void load_plane(uint32_t a_s, int slot, const __nv_bfloat16* src, const ConvArgs& a,
+                                           int x0, int y0, int z) {
+  z = z < 0 ? z + a.nz : (z >= a.nz ? z - a.nz : z);
+  const uint32_t base = a_s + slot * A_PLANE;
+  for (int i = threadIdx.x; i < HYT * HXT * 4; i += THREADS) {
+    const int c = i & 3;
+    const int s = i >> 2;
+    const int hx = s % HXT, hy = s / HXT;
+    int x = x0 + hx - 1, y = y0 + hy - 1;
+    x = x < 0 ? x + a.nx : (x >= a.nx ? x - a.nx : x);
+    y = y < 0 ? y + a.ny : (y >= a.ny ? y - a.ny : y);
+    cp16(base + hy * A_YROW + c * A_CHUNK + hx * 16, src + (((int64_t)z * a.ny + y) * a.nx + x) * 32 + c * 8);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int EPI, bool STORE_Z>
+__global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + B_BYTES + A_BYTES);  // [2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + B_BYTES + A_BYTES + 32);
+  volatile int* abort = reinterpret_cast<volatile int*>(sm + B_BYTES + A_BYTES + 48);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t b_s = su32(sm), a_s = su32(sm + B_BYTES);
+  const uint32_t mb[2] = {su32(mbar), su32(mbar + 1)};
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tslot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    *abort = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb[0]));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb[1]));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // weights [tap][co][ci] (global) -> [tap][ci chunk][co][8] (shared)
+  for (int i = tid; i < 27 * 32 * 4; i += THREADS) {
+    const int tap = i / 128, r = i % 128, n = r / 4, c = r % 4;
+    cp16(b_s + tap * B_TAP + c * B_CHUNK + n * 16, a.w + ((int64_t)tap * 32 + n) * 32 + c * 8);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  // epilogue geometry: warp w -> TMEM lanes 32 (w & 3) (sites), columns 16 (w >> 2) (channels)
+  const int quarter = warp & 3, half = warp >> 2;
+  float bias[16];
+#pragma unroll
+  for (int n = 0; n < 16; ++n) bias[n] = (EPI == EPI_GELU && a.bias) ? a.bias[16 * half + n] : 0.f;
+
+  const int tiles_x = a.nx / TCX, tiles_y = a.ny / TCR, zchunks = (a.nz + ZC - 1) / ZC;
+  const int64_t items_per = (int64_t)tiles_x * tiles_y * zchunks;
+  const int64_t nitems = items_per * a.nlat;
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  uint32_t phase[2] = {0, 0};
+  int pending[2] = {0, 0};  // commits not yet waited for, per TMEM buffer
+  bool failed = false;
+
+  auto epilogue = [&](int buf, int64_t lat_base, int x0, int y0, int z) {
+    const int x = x0 + 32 * quarter + lane;
+#pragma unroll 1
+    for (int r = 0; r < TCR; ++r) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + buf * 64 + r * 32 + 16 * half;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      const int64_t s = lat_base + ((int64_t)z * a.ny + (y0 + r)) * a.nx + x;
+      __align__(16) __nv_bfloat162 o[8];
+      if constexpr (EPI == EPI_GELU) {
+        __align__(16) __nv_bfloat162 zz[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float z0f = __uint_as_float(v[2 * j]) + bias[2 * j];
+          const float z1f = __uint_as_float(v[2 * j + 1]) + bias[2 * j + 1];
+          zz[j] = __floats2bfloat162_rn(z0f, z1f);
+          o[j] = __floats2bfloat162_rn(gelu_f(z0f), gelu_f(z1f));
+        }
+        if constexpr (STORE_Z) {
+          uint4* zp = reinterpret_cast<uint4*>(a.zout + s * 32 + 16 * half);
+          zp[0] = reinterpret_cast<const uint4*>(zz)[0];
+          zp[1] = reinterpret_cast<const uint4*>(zz)[1];
+        }
+      } else {  // EPI_BWD: times GELU'(z) of the layer's stored pre-activation
+        __align__(16) __nv_bfloat162 zz[8];
+        const uint4* zp = reinterpret_cast<const uint4*>(a.zin + s * 32 + 16 * half);
+        reinterpret_cast<uint4*>(zz)[0] = zp[0];
+        reinterpret_cast<uint4*>(zz)[1] = zp[1];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float g0 = gelu_df(__bfloat162float(zz[j].x)), g1 = gelu_df(__bfloat162float(zz[j].y));
+          o[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * g0, __uint_as_float(v[2 * j + 1]) * g1);
+        }
+      }
+      uint4* op = reinterpret_cast<uint4*>(a.out + s * 32 + 16 * half);
+      op[0] = reinterpret_cast<const uint4*>(o)[0];
+      op[1] = reinterpret_cast<const uint4*>(o)[1];
+    }
+  };
+
+  for (int64_t item = blockIdx.x; item < nitems && !failed; item += gridDim.x) {
+    const int64_t li = item / items_per;
+    int64_t rr = item % items_per;
+    const int tx = (int)(rr % tiles_x);
+    rr /= tiles_x;
+    const int ty = (int)(rr % tiles_y);
+    const int zc = (int)(rr / tiles_y);
+    const int x0 = tx * TCX, y0 = ty * TCR, zA = zc * ZC;
+    const int nzs = min(ZC, a.nz - zA);
+    const __nv_bfloat16* src = a.in + li * Nsite * 32;
+    const int64_t lat_base = li * Nsite;
+    // planes q = -1, 0, 1 of the item (q = z - zA) into slots (q + 1) & 3
+    load_plane(a_s, 0, src, a, x0, y0, zA - 1);
+    load_plane(a_s, 1, src, a, x0, y0, zA);
+    load_plane(a_s, 2, src, a, x0, y0, zA + 1);
+#pragma unroll 1
+    for (int j = 0; j <= nzs; ++j) {
+      const int buf = j & 1;
+      if (j < nzs) {
+        // planes j-1 .. j+1 have landed (only they are outstanding here)
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (*abort) {  // read after the barrier: every thread sees the same value
+          failed = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (tid == 0) {
+          // descriptors are affine in the start address: one base per operand and
+          // plane slot, compile-time offsets for the taps (the start-address field
+          // never carries: shared addresses stay below 256 KB)
+          const uint64_t bd0 = mdesc(b_s, B_CHUNK, CM_BYTES);
+#pragma unroll
+          for (int r = 0; r < TCR; ++r) {
+            const uint32_t d = tmem + buf * 64 + r * 32;
+            uint64_t ad0[3];
+#pragma unroll
+            for (int dz = 0; dz < 3; ++dz)
+              ad0[dz] = mdesc(a_s + ((j + dz) & 3) * A_PLANE + r * A_YROW, A_CHUNK, CM_BYTES);
+#pragma unroll
+            for (int tap = 0; tap < 27; ++tap) {
+              const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+              for (int k = 0; k < 2; ++k) {
+                const uint64_t ad = ad0[dz] + (uint64_t)((dy * A_YROW + dx * 16 + 2 * k * A_CHUNK) >> 4);
+                const uint64_t bd = bd0 + (uint64_t)((tap * B_TAP + 2 * k * B_CHUNK) >> 4);
+                mma_bf16(d, ad, bd, (tap | k) ? 1u : 0u);
+              }
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                           mb[buf])
+                       : "memory");
+        }
+        pending[buf] = 1;
+      }
+      if (j >= 1) {
+        const int pb = (j - 1) & 1;
+        // bounded wait, agreed within the warp (tcgen05.ld is warp-collective)
+        uint32_t spins = 0;
+        int to = 0;
+        while (!mbar_try(mb[pb], phase[pb])) {
+          if (++spins > kSpinLimit) {
+            to = 1;
+            break;
+          }
+        }
+        if (__any_sync(0xffffffffu, to)) {
+          if (lane == 0) *abort = 1;
+        } else {
+          phase[pb] ^= 1u;
+          pending[pb] = 0;
+          // the slot of plane j-2 is free: prefetch plane j+2 behind the epilogue
+          if (j + 2 <= nzs) load_plane(a_s, (j + 3) & 3, src, a, x0, y0, zA + j + 2);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          epilogue(pb, lat_base, x0, y0, zA + j - 1);
+        }
+        // TMEM buffer pb is read before MMA(j + 1) overwrites it
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (*abort) {
+          failed = true;
+          break;
+        }
+      } else if (2 <= nzs) {
+        // j == 0: slot 3 is free; prefetch plane 2
+        load_plane(a_s, 3, src, a, x0, y0, zA + 2);
+      }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(err, 1);
+    // MMAs of a buffer that was not waited for may still be running
+    for (int b = 0; b < 2; ++b) {
+      if (!pending[b]) continue;
+      uint32_t spins = 0;
+      while (!mbar_try(mb[b], phase[b]) && ++spins < kSpinLimit) {
+      }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+}  // namespace
+
+bool conv_tc_ok(int ca, int cb, int epi, int nx, int ny) {
+  return ca == 32 && cb == 32 && epi != EPI_LINEAR && nx % TCX == 0 && ny % TCR == 0;
+}
+
+int conv_tc(const ConvArgs& a, int epi, int nsm, int* err, cudaStream_t s) {
+  const bool sz = a.zout != nullptr;
+  auto go = [&](auto kern) -> int {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);
+    if (e != cudaSuccess) return cuda_fail(e, "tcgen05 conv smem attribute");
+    const int64_t nitems = (int64_t)(a.nx / TCX) * (a.ny / TCR) * ((a.nz + ZC - 1) / ZC) * a.nlat;
+    const unsigned grid = (unsigned)std::min<int64_t>(nitems, (int64_t)nsm);
+    kern<<<grid, THREADS, SMEM_TC, s>>>(a, err);
+    if (g_launch_counter) ++*g_launch_counter;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? LAT_OK : cuda_fail(e, "tcgen05 conv launch");
+  };
+  if (epi == EPI_GELU) return sz ? go(conv_tc_kernel<EPI_GELU, true>) : go(conv_tc_kernel<EPI_GELU, false>);
+  return go(conv_tc_kernel<EPI_BWD, false>);
+}
+
+}  // namespace net
+}  // namespace lat

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "net.hpp"
@@ -512,6 +513,11 @@ int conv_go(const ConvArgs& a, int nsm, cudaStream_t s) {
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s) {
   if (a.nx % TX || a.ny % TY || a.nz < 1) return set_error(LAT_ERR_ARG, "closure lattice: nx % 16, ny % 8");
+  static const bool no_tc = [] {
+    const char* v = getenv("LAT_NO_TCGEN05");
+    return v && v[0] && v[0] != '0';
+  }();
+  if (!no_tc && a.err && conv_tc_ok(ca, cb, epi, a.nx, a.ny)) return conv_tc(a, epi, nsm, a.err, s);
   const bool sz = a.zout != nullptr;
   if (ca == 8 && cb == 32 && epi == EPI_GELU) return sz ? conv_go<8, 32, EPI_GELU, true>(a, nsm, s)
                                                         : conv_go<8, 32, EPI_GELU, false>(a, nsm, s);

@@ -46,6 +46,7 @@ struct lat_net_s {
   int32_t* idx = nullptr;
   int idx_cap = 0;
   int64_t launches = 0;
+  int* err = nullptr;  // device error word of the tensor-memory convolutions (bounded waits)
 };
 
 namespace {
@@ -121,6 +122,7 @@ int check_lattice(int nx, int ny, int nz) {
 int forward(lat_net_s* n, const InferBufs& b, int nx, int ny, int nz, int64_t nlat, bool store_z, cudaStream_t s) {
   ConvArgs c{};
   c.nx = nx; c.ny = ny; c.nz = nz; c.nlat = nlat;
+  c.err = n->err;
   c.in = b.a0; c.w = n->wf1; c.bias = n->P + OFF_B1; c.out = b.a1; c.zout = store_z ? b.z1 : nullptr;
   NRET(conv(c, C_IN, C_HID, EPI_GELU, n->nsm, s));
   c.in = b.a1; c.w = n->wf2; c.bias = n->P + OFF_B2; c.out = b.a2; c.zout = store_z ? b.z2 : nullptr;
@@ -181,6 +183,7 @@ int loss_and_grad(lat_net_s* n, const float* data, int64_t stride, int nidx, int
   NRET(wgrad(w, C_HID, C_OUT, nblk, n->G + OFF_W3, n->G + OFF_B3, s));
   ConvArgs c{};
   c.nx = nx; c.ny = ny; c.nz = nz; c.nlat = nidx;
+  c.err = n->err;
   c.in = n->d3; c.w = n->wb3; c.zin = n->z2; c.out = n->d2;
   NRET(conv(c, C_OUT, C_HID, EPI_BWD, n->nsm, s));
   // layer 2
@@ -195,6 +198,19 @@ int loss_and_grad(lat_net_s* n, const float* data, int64_t stride, int nidx, int
     NCK(cudaMemcpyAsync(loss, n->lsum, sizeof(double), cudaMemcpyDeviceToHost, s));
   }
   NCK(cudaStreamSynchronize(s));
+  return LAT_OK;
+}
+
+// the error word of the bounded waits, read after the stream has drained
+int check_err(lat_net_s* n) {
+  int h = 0;
+  NCK(cudaMemcpyAsync(&h, n->err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+  NCK(cudaStreamSynchronize(n->stream));
+  if (h) {
+    cudaMemsetAsync(n->err, 0, sizeof(int), n->stream);
+    cudaStreamSynchronize(n->stream);
+    return set_error(LAT_ERR_TIMEOUT, "closure convolution: a tensor-core wait gave up");
+  }
   return LAT_OK;
 }
 
@@ -239,6 +255,8 @@ void out_scale(const lat_net_s* n, double out[2]) {
 
 int net_device(const lat_net_s* n) { return n->dev; }
 
+int* net_err(const lat_net_s* n) { return n->err; }
+
 }  // namespace net
 }  // namespace lat
 
@@ -275,8 +293,10 @@ int lat_net_create(lat_net_t** out, int32_t device, uint64_t seed) {
   if ((e = cudaMalloc(&n->part, (size_t)nblk * 27 * C_HID * C_HID * sizeof(float))) != cudaSuccess ||
       (e = cudaMalloc(&n->part_b, (size_t)nblk * C_HID * sizeof(float))) != cudaSuccess ||
       (e = cudaMalloc(&n->lpart, (size_t)2 * n->nsm * sizeof(double))) != cudaSuccess ||
-      (e = cudaMalloc(&n->lsum, sizeof(double))) != cudaSuccess)
+      (e = cudaMalloc(&n->lsum, sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&n->err, sizeof(int))) != cudaSuccess)
     return bail(cuda_fail(e, "training scratch"));
+  cudaMemsetAsync(n->err, 0, sizeof(int), n->stream);
   // He-normal initial weights (Box-Muller on a splitmix64 stream); the last
   // layer starts 100x smaller so the untrained closure is close to zero.
   // Padded channels (inputs 4..7, outputs 2..7) stay zero.
@@ -311,7 +331,7 @@ int lat_net_destroy(lat_net_t* n) {
   if (n->stream) cudaStreamSynchronize(n->stream);
   free_acts(n);
   void* ps[] = {n->P, n->G, n->m, n->v, n->wf1, n->wf2, n->wf3, n->wb2, n->wb3,
-                n->part, n->part_b, n->lpart, n->lsum, n->idx};
+                n->part, n->part_b, n->lpart, n->lsum, n->idx, n->err};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (n->stream) cudaStreamDestroy(n->stream);
@@ -372,8 +392,7 @@ int lat_net_forward(lat_net_t* n, const float* data, int64_t stride, const int32
   InferBufs b = train_bufs(n);
   b.out = out_dev;
   NRET(forward(n, b, nx, ny, nz, nidx, false, n->stream));
-  NCK(cudaStreamSynchronize(n->stream));
-  return LAT_OK;
+  return check_err(n);
 }
 
 int lat_net_grad(lat_net_t* n, const float* data, int64_t stride, const int32_t* idx, int32_t nidx, int32_t nx,
@@ -382,6 +401,7 @@ int lat_net_grad(lat_net_t* n, const float* data, int64_t stride, const int32_t*
   Guard g(n);
   NRET(batch_args(n, data, stride, idx, nidx, nx, ny, nz));
   NRET(loss_and_grad(n, data, stride, nidx, nx, ny, nz, loss));
+  NRET(check_err(n));
   if (grad_host) {
     NCK(cudaMemcpyAsync(grad_host, n->G, (size_t)N_PARAMS * sizeof(float), cudaMemcpyDeviceToHost, n->stream));
     NCK(cudaStreamSynchronize(n->stream));
@@ -399,8 +419,7 @@ int lat_net_train_step(lat_net_t* n, const float* data, int64_t stride, const in
   n->step += 1;
   NRET(adam(n->P, n->G, n->m, n->v, N_PARAMS, lr, n->step, n->stream));
   NRET(repack_all(n, n->stream));
-  NCK(cudaStreamSynchronize(n->stream));
-  return LAT_OK;
+  return check_err(n);
 }
 
 int64_t lat_net_launch_count(const lat_net_t* n) { return n ? n->launches : -1; }
@@ -417,6 +436,7 @@ int lat_net_time_forward(lat_net_t* n, int32_t nx, int32_t ny, int32_t nz, int32
   InferBufs b = train_bufs(n);
   ConvArgs c{};
   c.nx = nx; c.ny = ny; c.nz = nz; c.nlat = 1;
+  c.err = n->err;
   double acc[4] = {0, 0, 0, 0};
   int st = LAT_OK;
   for (int r = 0; r <= reps && st == LAT_OK; ++r) {  // r = 0 is a warm-up
@@ -450,6 +470,7 @@ int lat_net_time_forward(lat_net_t* n, int32_t nx, int32_t ny, int32_t nz, int32
   }
   for (auto& e : ev) cudaEventDestroy(e);
   if (st != LAT_OK) return st;
+  NRET(check_err(n));
   for (int q = 0; q < 4; ++q) ms[q] = acc[q] / reps;
   return LAT_OK;
 }

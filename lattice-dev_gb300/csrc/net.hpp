@@ -28,6 +28,7 @@ struct ConvArgs {
   __nv_bfloat16* zout;          // pre-activation (GELU, optional)
   const __nv_bfloat16* zin;     // pre-activation of the layer (BWD)
   float* outf;                  // [nlat][N][2] (LINEAR)
+  int* err;                     // device error word (bounded waits of the tensor-memory kernel)
 };
 
 struct WgradArgs {
@@ -81,8 +82,12 @@ int infer(lat_net_s* n, const void* const ch[4], int fp64, int nx, int ny, int n
           const InferBufs& b, cudaStream_t s);
 void out_scale(const lat_net_s* n, double out[2]);
 int net_device(const lat_net_s* n);
+int* net_err(const lat_net_s* n);
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s);
+// 32 -> 32 channel layers on tcgen05 (k_conv_tc.cu): nx % 128 == 0, ny % 2 == 0
+bool conv_tc_ok(int ca, int cb, int epi, int nx, int ny);
+int conv_tc(const ConvArgs& a, int epi, int nsm, int* err, cudaStream_t s);
 int wgrad_blocks(int nsm);
 int wgrad(const WgradArgs& a, int cx, int cd, int nblk, float* dW, float* db, cudaStream_t s);
 int pack(const PackArgs& a, int fp64, int nsm, cudaStream_t s);

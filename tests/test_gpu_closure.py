@@ -39,14 +39,17 @@ def _net(engine, seed, scale_last=1.0):
     return net, q.astype(np.float64), norm
 
 
-SHAPE = (16, 8, 4)
+# (16, 8, 4): every layer on the mma.sync kernels; (128, 8, 2): the 32 -> 32
+# layer (forward and backward data) on the tcgen05 / tensor-memory kernel
+SHAPES = [(16, 8, 4), (128, 8, 2)]
 
 
-def test_forward_matches_oracle(engine):
+@pytest.mark.parametrize("SHAPE", SHAPES)
+def test_forward_matches_oracle(engine, SHAPE):
     host, buf = _dataset(engine, SHAPE, 3, 1)
     net, p, norm = _net(engine, 7)
     idx = [2, 0]
-    out = net.forward(buf, 6 * 16 * 8 * 4, idx, SHAPE)
+    out = net.forward(buf, 6 * int(np.prod(SHAPE)), idx, SHAPE)
     x = NO.pack_inputs(host[idx], norm[0], norm[1], emulate=True)
     ref_e, _ = NO.forward(p, x, emulate=True)
     ref, _ = NO.forward(p, NO.pack_inputs(host[idx], norm[0], norm[1]))
@@ -58,11 +61,12 @@ def test_forward_matches_oracle(engine):
     assert rel_err(out, ref) <= 3e-2
 
 
-def test_gradients_match_oracle(engine):
+@pytest.mark.parametrize("SHAPE", SHAPES)
+def test_gradients_match_oracle(engine, SHAPE):
     """The hand-written backward kernels against the oracle's exact gradient."""
     host, buf = _dataset(engine, SHAPE, 2, 2)
     net, p, norm = _net(engine, 9)
-    loss, g = net.grad(buf, 6 * 16 * 8 * 4, [1, 0], SHAPE)
+    loss, g = net.grad(buf, 6 * int(np.prod(SHAPE)), [1, 0], SHAPE)
     lref_e, gref_e = NO.loss_and_grad(p, host[[1, 0]], norm, emulate=True)
     lref, gref = NO.loss_and_grad(p, host[[1, 0]], norm)
     assert abs(loss - lref_e) <= 1e-3 * lref_e
