@@ -290,7 +290,7 @@ int lat_ens_tuning_get(const lat_ens_t* e, int32_t out[2]);
 /* ------------------------------------------------- learned subgrid closure */
 /* No reference counterpart.  A coarse lattice evolved with a kick corrected
  * by a small network: three periodic 3x3x3 convolutions 4 -> 32 -> 32 -> 2
- * channels with GELU after the first two, BF16 weights and activations,
+ * channels with GELU (tanh form) after the first two, BF16 weights and activations,
  * FP32 accumulation on the tensor cores, FP32 master weights and Adam state.
  * Inputs are the coarse (phi, chi, pi_phi, pi_chi) of a two-field lattice,
  * normalised as (x - in_shift) * in_scale; the output o_f gives the force

@@ -14,11 +14,11 @@
 //   A: the 128 rows of one tap are 128 consecutive x of one halo row (core
 //      matrices 128 B apart); the tap's x offset is a 16-byte shift;
 //   B: the weights [tap 27][channel chunk 4][out 32][8], staged once.
-// Accumulators are double-buffered in TMEM (2 x 64 columns): the MMAs of
-// step j run while eight warps read back step j-1 (tcgen05.ld; warp w owns
-// TMEM lanes 32 (w mod 4) .. and columns 16 (w / 4) ..) for the epilogue
-// (bias + GELU, or times GELU' for the backward data pass) and the next
-// plane's copies are in flight.
+// Accumulators are double-buffered in TMEM (2 x 64 columns): a ninth warp
+// issues the MMAs of step j while eight warps read back step j-1
+// (tcgen05.ld; warp w owns TMEM lanes 32 (w mod 4) .. and columns
+// 16 (w / 4) ..) for the epilogue (bias + GELU, or times GELU' for the
+// backward data pass) and the next plane's copies are in flight.
 //
 // Every wait is bounded: a warp that gives up raises a shared abort flag that
 // the whole block reads after its next barrier; the block then sets the error
@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "gelu.cuh"
 #include "net.hpp"
 
 namespace lat {
@@ -48,7 +49,8 @@ constexpr int B_BYTES = 27 * B_TAP;                // 55 296
 constexpr int A_BYTES = NSLOT * A_PLANE;           // 133 120
 constexpr int TMEM_COLS = 128;                     // 2 buffers x 2 rows x 32 fp32 columns
 constexpr int SMEM_TC = B_BYTES + A_BYTES + 64;    // + two mbarriers and the TMEM address
-constexpr int THREADS = 256;
+constexpr int THREADS = 288;   // warps 0-7: copies and epilogue; warp 8: MMA issue
+constexpr int WORKERS = 256;
 constexpr uint32_t kSpinLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -87,17 +89,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t phase) {
   return ok != 0;
 }
 
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_df(float z) {
-  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
-}
+__device__ __forceinline__ float gelu_f(float z) { return gelu_t(z); }
+__device__ __forceinline__ float gelu_df(float z) { return gelu_t_d(z); }
 
 // copies of halo plane z (periodic) of an item into ring slot `slot`
 __device__ __forceinline__ void load_plane(uint32_t a_s, int slot, const __nv_bfloat16* src, const ConvArgs& a,
                                            int x0, int y0, int z) {
   z = z < 0 ? z + a.nz : (z >= a.nz ? z - a.nz : z);
   const uint32_t base = a_s + slot * A_PLANE;
-  for (int i = threadIdx.x; i < HYT * HXT * 4; i += THREADS) {
+  if (threadIdx.x >= WORKERS) return;  // the MMA warp issues no copies
+  for (int i = threadIdx.x; i < HYT * HXT * 4; i += WORKERS) {
     const int c = i & 3;
     const int s = i >> 2;
     const int hx = s % HXT, hy = s / HXT;
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
   const int quarter = warp & 3, half = warp >> 2;
   float bias[16];
 #pragma unroll
-  for (int n = 0; n < 16; ++n) bias[n] = (EPI == EPI_GELU && a.bias) ? a.bias[16 * half + n] : 0.f;
+  for (int n = 0; n < 16; ++n) bias[n] = (EPI == EPI_GELU && a.bias && warp < 8) ? a.bias[16 * half + n] : 0.f;
 
   const int tiles_x = a.nx / TCX, tiles_y = a.ny / TCR, zchunks = (a.nz + ZC - 1) / ZC;
   const int64_t items_per = (int64_t)tiles_x * tiles_y * zchunks;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (tid == 0) {
+        if (warp == 8 && lane == 0) {
           // descriptors are affine in the start address: one base per operand and
           // plane slot, compile-time offsets for the taps (the start-address field
           // never carries: shared addresses stay below 256 KB)
@@ -260,16 +261,19 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
       }
       if (j >= 1) {
         const int pb = (j - 1) & 1;
-        // bounded wait, agreed within the warp (tcgen05.ld is warp-collective)
+        // bounded wait, agreed within the warp (tcgen05.ld is warp-collective);
+        // the MMA warp goes straight to the barrier
         uint32_t spins = 0;
         int to = 0;
-        while (!mbar_try(mb[pb], phase[pb])) {
+        while (warp < 8 && !mbar_try(mb[pb], phase[pb])) {
           if (++spins > kSpinLimit) {
             to = 1;
             break;
           }
         }
-        if (__any_sync(0xffffffffu, to)) {
+        if (warp == 8) {
+          // no TMEM reads, no copies
+        } else if (__any_sync(0xffffffffu, to)) {
           if (lane == 0) *abort = 1;
         } else {
           phase[pb] ^= 1u;
@@ -296,8 +300,9 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
   }
   if (failed) {
     if (tid == 0) atomicOr(err, 1);
-    // MMAs of a buffer that was not waited for may still be running
-    for (int b = 0; b < 2; ++b) {
+    // MMAs of a buffer that was not waited for may still be running (the
+    // worker warps track the phases; the MMA warp does not wait)
+    for (int b = 0; b < 2 && warp < 8; ++b) {
       if (!pending[b]) continue;
       uint32_t spins = 0;
       while (!mbar_try(mb[b], phase[b]) && ++spins < kSpinLimit) {

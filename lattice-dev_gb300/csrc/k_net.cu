@@ -20,6 +20,7 @@
 #include <cstdlib>
 
 #include "common.cuh"
+#include "gelu.cuh"
 #include "net.hpp"
 
 namespace lat {
@@ -77,11 +78,8 @@ __device__ __forceinline__ void mma1688(float (&d)[4], const uint32_t (&a)[2], u
                : "r"(a[0]), "r"(a[1]), "r"(b0));
 }
 
-// GELU with the error function, and its derivative
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_d(float z) {
-  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
-}
+__device__ __forceinline__ float gelu(float z) { return gelu_t(z); }
+__device__ __forceinline__ float gelu_d(float z) { return gelu_t_d(z); }
 
 // padded shared-memory row (elements) of a site with C channels: 80-byte rows
 // for 32 channels keep the 8 rows of an ldmatrix in distinct banks

@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: CPU FP64 restatement of the closure network.
 
 Checker for the GPU closure kernels (BF16 tensor-core convolutions): the same
-three periodic 3x3x3 convolutions 4 -> 32 -> 32 -> 2 with GELU, the same
+three periodic 3x3x3 convolutions 4 -> 32 -> 32 -> 2 with GELU (tanh form), the same
 mean-squared-error loss and its exact gradient, in numpy float64.  The
 network has no counterpart in the reference; its definition is the one in
 include/lattice.h (lat_net_*).  Optionally the BF16 rounding points of the GPU
@@ -15,7 +15,6 @@ W3[27][32][8] b3[8]; tap = (dz+1)*9 + (dy+1)*3 + (dx+1) for the input offset
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 C_IN, C_HID, C_OUT = 8, 32, 8
 SHAPES = [("W1", (27, C_IN, C_HID)), ("b1", (C_HID,)), ("W2", (27, C_HID, C_HID)), ("b2", (C_HID,)),
@@ -45,12 +44,17 @@ def bf16(x: np.ndarray) -> np.ndarray:
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+_C = np.sqrt(2.0 / np.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU in its tanh form (the network's activation)."""
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + 0.044715 * z ** 3)))
 
 
 def gelu_d(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def _shift(a, off):
