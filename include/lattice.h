@@ -248,6 +248,17 @@ int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0,
  * init_fields/initbubble, Discrete/Bubble-Collisions/ic_bubble.f90:17-123. */
 int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres,
                      double radius, double width);
+/* Expanding-wall bubbles exactly as init_fields / initbubble build them
+ * (Discrete/Bubble-Collisions/ic_bubble.f90:17-77 with the profile and
+ * derivative of init_cond.f90:192-234): for each bubble centred at the
+ * 1-based site (cx, cy, cz), with r the unwrapped distance and
+ * step = (phi_false - phi_true)/2, ave = (phi_true - phi_false)/2:
+ *   r > t0:  phi += step tanh(s/sqrt2) + ave,  s = sqrt(r^2 - t0^2) - r0,
+ *            pi  += -step t0 / (sqrt(r^2 - t0^2) sqrt2) / cosh^2(s/sqrt2);
+ *   else:    phi += phi_true - phi_false;
+ * then phi += phi_false.  Other fields are zero. */
+int lat_init_bubbles_boosted(lat_t* h, int32_t nbub, const int32_t* centres, double r0, double t0,
+                             double phi_false, double phi_true);
 
 /* -------------------------------------------------------------- checkpoint */
 /* Raw native-double checkpoint fld_<i>.raw / fldp_<i>.raw (interior only,
@@ -256,6 +267,20 @@ int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres,
  * and driver.f90:71-91,117-129.  `dir` must exist. */
 int lat_checkpoint_write(lat_t* h, const char* dir, double time, int32_t frame);
 int lat_checkpoint_read(lat_t* h, const char* dir, double* time, int32_t* frame);
+
+/* ------------------------------------------------------------ output files */
+/* Appends one record to an energy file in the column layout of dump_rho
+ * (Pseudospec/openmp_dev/evolve_spectral.f90:402-405, energy_spec.out):
+ * time, a, rho, KE, PE, GE, -3H^2, (rho - 3H^2)/rho, -ysclp^2/(12 a^4),
+ * <phi_1>, <phi_2> (the last for two or more fields), each as Fortran
+ * ES22.15 followed by two spaces. */
+int lat_write_energy_line(lat_t* h, const char* path, double time);
+/* Appends one block to a spectrum file as make_output writes it
+ * (evolve_spectral.f90:525-549, spectrum.out): for each of the ns bins,
+ * (i-1) dk, P(phi_1), P(pi_1), Re and Im of the pi_1 x conj(phi_1) cross
+ * spectrum, then zeros up to 2 nfld + 2 columns (columns the reference
+ * leaves unset), then an empty line. */
+int lat_write_spectrum_block(lat_t* h, const char* path);
 
 /* ------------------------------------------------------------- ensembles */
 /* A batch of independent runs of one model on lattices of uneven size,

@@ -104,6 +104,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_gw_spectrum": ([P, I, dp, dp], I), "lat_gw_download": ([P, dp, dp], I),
         "lat_gw_upload": ([P, dp, dp], I),
         "lat_init_vacuum": ([P, U64, dp, dp, dp, D, D], I), "lat_init_bubbles": ([P, I, dp, D, D], I),
+        "lat_init_bubbles_boosted": ([P, I, C.POINTER(I), D, D, D, D], I),
         "lat_checkpoint_write": ([P, C.c_char_p, D, I], I),
         "lat_checkpoint_read": ([P, C.c_char_p, dp, C.POINTER(I)], I),
         "lat_ens_create": ([C.POINTER(P), C.POINTER(LatConfig), I, C.POINTER(I)], I),
@@ -128,6 +129,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_net_grad": ([P, P, I64, C.POINTER(I), I, I, I, I, dp, C.POINTER(C.c_float)], I),
         "lat_net_train_step": ([P, P, I64, C.POINTER(I), I, I, I, I, D, dp], I),
         "lat_net_launch_count": ([P], I64), "lat_net_time_forward": ([P, I, I, I, I, dp], I),
+        "lat_write_energy_line": ([P, C.c_char_p, D], I), "lat_write_spectrum_block": ([P, C.c_char_p], I),
         "lat_closure_attach": ([P, P, I, I], I), "lat_coarsen": ([P, I, I, P], I),
     }
     for name, (args, res) in sig.items():
@@ -336,6 +338,13 @@ class Lattice:
         _check(_lib.lat_init_bubbles(self._h, c.shape[0], _dp(c), radius, width))
 
     # checkpoint ----------------------------------------------------------------
+    def init_bubbles_boosted(self, centres, r0, t0, phi_false, phi_true) -> None:
+        """Expanding-wall bubbles as the reference's initbubble builds them
+        (centres: 1-based site indices (x, y, z) per bubble)."""
+        c = np.ascontiguousarray(np.asarray(centres, dtype=np.int32).reshape(-1, 3))
+        _check(_lib.lat_init_bubbles_boosted(self._h, len(c), c.ctypes.data_as(C.POINTER(C.c_int32)), r0, t0,
+                                             phi_false, phi_true))
+
     def checkpoint_write(self, directory, time=0.0, frame=0) -> None:
         _check(_lib.lat_checkpoint_write(self._h, str(directory).encode(), time, frame))
 
@@ -381,6 +390,13 @@ class Lattice:
         out = (C.c_int32 * 6)()
         _check(_lib.lat_tuning_get(self._h, out))
         return list(out)
+
+    # output files in the reference's column layouts
+    def write_energy_line(self, path, time: float) -> None:
+        _check(_lib.lat_write_energy_line(self._h, str(path).encode(), time))
+
+    def write_spectrum_block(self, path) -> None:
+        _check(_lib.lat_write_spectrum_block(self._h, str(path).encode()))
 
     # learned closure
     def coarsen(self, nc: int, out: "DeviceArray", offset: int = 0, units: int = 0) -> None:

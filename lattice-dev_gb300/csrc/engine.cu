@@ -1370,6 +1370,30 @@ int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres, double radiu
   return LAT_OK;
 }
 
+int lat_init_bubbles_boosted(lat_t* h, int32_t nbub, const int32_t* centres, double r0, double t0,
+                             double phi_false, double phi_true) {
+  if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(r0 >= 0) || !(t0 >= 0))
+    return set_error(LAT_ERR_ARG, "bad bubble arguments");
+  ApiGuard g(h);
+  RET(ensure_stage(h, (size_t)std::max(h->nf, 2) * h->N + 3 * 64));
+  double* phi = h->stage;
+  double* pi = h->stage + h->N;
+  int* cen = reinterpret_cast<int*>(h->stage + (size_t)std::max(h->nf, 2) * h->N);
+  if (nbub > 0) CK(cudaMemcpyAsync(cen, centres, sizeof(int32_t) * 3 * nbub, cudaMemcpyHostToDevice, h->stream));
+  RET(launch_bubbles_boosted(phi, pi, h->nx, h->ny, h->nz, h->dx, nbub, cen, r0, t0, phi_false, phi_true,
+                             h->stream));
+  const size_t fb = (size_t)h->N * h->rsz;
+  RET(launch_from_fp64(phi, h->N, h->prec, h->fld[h->cur], h->fldc, h->stream));
+  RET(launch_from_fp64(pi, h->N, h->prec, h->fldp, nullptr, h->stream));
+  for (int l = 1; l < h->nf; ++l) {
+    CK(cudaMemsetAsync((char*)h->fld[h->cur] + l * fb, 0, fb, h->stream));
+    if (h->fldc) CK(cudaMemsetAsync((char*)h->fldc + l * fb, 0, fb, h->stream));
+    CK(cudaMemsetAsync((char*)h->fldp + l * fb, 0, fb, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return LAT_OK;
+}
+
 int lat_checkpoint_write(lat_t* h, const char* dir, double time, int32_t frame) {
   if (!h || !dir) return set_error(LAT_ERR_ARG, "null argument");
   std::vector<double> f((size_t)h->nf * h->N), p((size_t)h->nf * h->N);
@@ -1838,6 +1862,50 @@ int lat_coarsen(lat_t* h, int32_t nc, int32_t units, float* out) {
   if (phic) cudaFree(phic);
   if (tmp) cudaFree(tmp);
   return st;
+}
+
+// One Fortran ES22.15 field followed by the 2X of the reference's
+// '(30(ES22.15,2X))' records.
+static void put_es(FILE* fp, double v) { fprintf(fp, "%22.15E  ", v); }
+
+int lat_write_energy_line(lat_t* h, const char* path, double time) {
+  if (!h || !path) return set_error(LAT_ERR_ARG, "null argument");
+  double e[LAT_NENERGY];
+  RET(lat_energies(h, e));
+  ApiGuard g(h);
+  FILE* fp = fopen(path, "a");
+  if (!fp) return set_error(LAT_ERR_IO, std::string("cannot open ") + path);
+  const double a = e[LAT_E_A], ap = e[LAT_E_AP];
+  const double cols[11] = {time, a, e[LAT_E_RHO], e[LAT_E_KE], e[LAT_E_PE], e[LAT_E_GE_LAP], e[LAT_E_GRAV],
+                           (e[LAT_E_RHO] + e[LAT_E_GRAV]) / e[LAT_E_RHO], -ap * ap / 12.0 / (a * a * a * a),
+                           e[LAT_E_MEAN0], e[LAT_E_MEAN1]};
+  const int n = h->nf >= 2 ? 11 : 10;
+  for (int i = 0; i < n; ++i) put_es(fp, cols[i]);
+  fputc('\n', fp);
+  const bool ok = fclose(fp) == 0;
+  return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);
+}
+
+int lat_write_spectrum_block(lat_t* h, const char* path) {
+  if (!h || !path) return set_error(LAT_ERR_ARG, "null argument");
+  int32_t ns = 0;
+  RET(lat_spectrum_nbins(h, &ns));
+  std::vector<double> S1(ns), S2(ns), Cr(ns), Ci(ns), W(ns);
+  RET(lat_spectrum(h, LAT_SPEC_FLD, 0, LAT_SPEC_WEIGHTED, ns, S1.data(), W.data()));
+  RET(lat_spectrum(h, LAT_SPEC_FLDP, 0, LAT_SPEC_WEIGHTED, ns, S2.data(), W.data()));
+  RET(lat_crossspec(h, LAT_SPEC_FLDP, 0, LAT_SPEC_FLD, 0, ns, Cr.data(), Ci.data()));
+  FILE* fp = fopen(path, "a");
+  if (!fp) return set_error(LAT_ERR_IO, std::string("cannot open ") + path);
+  const int ncols = 2 * h->nf + 2;  // the reference fills the first four
+  for (int i = 0; i < ns; ++i) {
+    put_es(fp, i * h->dkx);
+    const double v[4] = {S1[i], S2[i], Cr[i], Ci[i]};
+    for (int c = 0; c < ncols; ++c) put_es(fp, c < 4 ? v[c] : 0.0);
+    fputc('\n', fp);
+  }
+  fputc('\n', fp);
+  const bool ok = fclose(fp) == 0;
+  return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);
 }
 
 int lat_tuning_get(const lat_t* h, int32_t out[6]) {

@@ -184,6 +184,8 @@ int launch_fd_laplacian64(const double* in, double* out, int nx, int ny, int nz,
 int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStream_t s);
 int launch_bubbles(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* centres_dev,
                    double radius, double width, cudaStream_t s);
+int launch_bubbles_boosted(double* phi, double* pi, int nx, int ny, int nz, double dx, int nbub, const int* cen,
+                           double r0, double t0, double pf, double pt, cudaStream_t s);
 
 // ------------------------------------------- coarsening (k_coarse.cu)
 int launch_truncate(const double2* Ff, int fnx, int fny, int fnz, double2* Fc, int nc, double scale, cudaStream_t s);

@@ -404,7 +404,42 @@ __global__ void bubbles_kernel(double* phi, int nx, int ny, int nz, double dx, i
   }
 }
 
+// Boosted-wall bubbles of Discrete/Bubble-Collisions/ic_bubble.f90:45-77 with
+// the profile and time derivative of init_cond.f90:192-234: centres are
+// 1-based site indices, distances are not wrapped, bubbles superpose, and
+// phi_false is added at the end.
+__global__ void bubbles_boost_kernel(double* phi, double* pi, int nx, int ny, int nz, double dx, int nbub,
+                                     const int* cen, double r0, double t0, double pf, double pt) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const double step = (pf - pt) / 2.0, ave = (-pf + pt) / 2.0, rt2 = 1.4142135623730951;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % nx), y = (int)((t / nx) % ny), z = (int)(t / ((int64_t)nx * ny));
+    double f = 0.0, d = 0.0;
+    for (int b = 0; b < nbub; ++b) {
+      const int ii = x + 1 - cen[3 * b], jj = y + 1 - cen[3 * b + 1], kk = z + 1 - cen[3 * b + 2];
+      const double rad = sqrt((double)(ii * ii + jj * jj + kk * kk) * dx * dx);
+      if (rad * rad > t0 * t0) {
+        const double s1 = sqrt(rad * rad - t0 * t0), s = s1 - r0;
+        const double ch = cosh(s / rt2);
+        f += step * tanh(s / rt2) + ave;
+        d += -step * t0 / s1 / rt2 / (ch * ch);
+      } else {
+        f += pt - pf;
+      }
+    }
+    phi[t] = f + pf;
+    pi[t] = d;
+  }
+}
+
 }  // namespace
+
+int launch_bubbles_boosted(double* phi, double* pi, int nx, int ny, int nz, double dx, int nbub, const int* cen,
+                           double r0, double t0, double pf, double pt, cudaStream_t s) {
+  bubbles_boost_kernel<<<grid_for((int64_t)nx * ny * nz), 256, 0, s>>>(phi, pi, nx, ny, nz, dx, nbub, cen, r0, t0,
+                                                                       pf, pt);
+  return done("boosted bubbles");
+}
 
 int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c, cudaStream_t s) {
   if (precision == LAT_FP64) aos2soa_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, (double*)hi, nullptr);

@@ -326,3 +326,75 @@ def test_prepared_graph_leaves_state_and_replays(engine):
         g.close()
     assert np.array_equal(out[0][0][0], out[1][0][0]) and np.array_equal(out[0][0][1], out[1][0][1])
     assert out[0][1] == out[1][1]
+
+
+def test_output_files_reference_layout(engine, tmp_path):
+    """energy_spec.out and spectrum.out records in the reference's column
+    layout (ES22.15 + 2X fields), with the values of the engine's reductions."""
+    n = 16
+    c = L.make_config(n, nfld=2, length=8.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g = engine.Lattice(c)
+    f, p = random_state((2, n, n, n), seed=31, mean=0.7, amp=0.1)
+    g.set_state(f, p)
+    g.set_scale_factor(1.0, 0.0)
+    g.calc_metric()
+    ef, sf = tmp_path / "energy_spec.out", tmp_path / "spectrum.out"
+    g.write_energy_line(ef, 0.0)
+    g.symp(4, 0.02, 3)
+    g.write_energy_line(ef, 0.06)
+    g.write_spectrum_block(sf)
+    lines = ef.read_text().splitlines()
+    assert len(lines) == 2
+    for ln in lines:
+        assert len(ln) == 11 * 24
+        assert all(ln[24 * i + 22:24 * i + 24] == "  " for i in range(11))
+    row = np.array([float(ln[24 * i:24 * i + 22]) for i in range(11) for ln in lines[1:]])
+    e = g.energies()
+    a, ap = g.scale_factor()
+    ref = [0.06, a, e[L.E_RHO], e[L.E_KE], e[L.E_PE], e[L.E_GE_LAP], e[L.E_GRAV],
+           (e[L.E_RHO] + e[L.E_GRAV]) / e[L.E_RHO], -ap * ap / 12 / a ** 4, e[L.E_MEAN0], e[L.E_MEAN1]]
+    assert np.allclose(row, ref, rtol=1e-14, atol=1e-300)
+    assert abs(row[6] - row[8]) <= 1e-12 * abs(row[6])  # -3H^2 printed twice, two formulas
+    blk = sf.read_text().split("\n")
+    ns = g.nbins()
+    assert blk[ns] == "" and len(blk[0]) == 7 * 24
+    tab = np.array([[float(ln[24 * i:24 * i + 22]) for i in range(7)] for ln in blk[:ns]])
+    S1, _ = g.spectrum(L.SPEC_FLD, 0, L.SPEC_WEIGHTED, ns)
+    S2, _ = g.spectrum(L.SPEC_FLDP, 0, L.SPEC_WEIGHTED, ns)
+    Cr, Ci = g.crossspec_3d(L.SPEC_FLDP, 0, L.SPEC_FLD, 0, ns)
+    assert np.allclose(tab[:, 0], np.arange(ns) * 2 * math.pi / 8.0, rtol=1e-15)
+    for col, ref in ((1, S1), (2, S2), (3, Cr), (4, Ci)):
+        assert np.allclose(tab[:, col], ref, rtol=1e-14, atol=0), col
+    assert np.all(tab[:, 5:] == 0)
+
+
+def test_boosted_bubbles_match_restatement(engine):
+    """lat_init_bubbles_boosted against a numpy restatement of
+    ic_bubble.f90 init_fields/initbubble with the init_cond.f90 profile,
+    centres at the reference's getbubpos positions (n/2 +- n/5)."""
+    n, dx = 32, 0.25
+    c = L.make_config(n, nfld=1, length=n * dx, laplacian=L.LAP_FD27, model=L.MODEL_DOUBLE_WELL,
+                      model_params=(0.01,), split_order=L.SPLIT_DEFROST)
+    g = engine.Lattice(c)
+    cen = [[n // 2 + n // 5, n // 2, n // 2], [n // 2 - n // 5, n // 2, n // 2]]
+    r0, pf, pt = 2.0, -1.0, 1.0
+    t0 = 1.3 * r0
+    g.init_bubbles_boosted(cen, r0, t0, pf, pt)
+    f, p = g.get_state()
+    i = np.arange(1, n + 1)
+    K, J, I = np.meshgrid(i, i, i, indexing="ij")
+    step, ave = (pf - pt) / 2, (-pf + pt) / 2
+    ef = np.zeros((n, n, n))
+    ep = np.zeros((n, n, n))
+    for cx, cy, cz in cen:
+        rad = np.sqrt(((I - cx) ** 2 + (J - cy) ** 2 + (K - cz) ** 2) * dx * dx)
+        out = rad ** 2 > t0 ** 2
+        s1 = np.sqrt(np.where(out, rad ** 2 - t0 ** 2, 1.0))
+        s = s1 - r0
+        ef += np.where(out, step * np.tanh(s / np.sqrt(2)) + ave, pt - pf)
+        ep += np.where(out, -step * t0 / s1 / np.sqrt(2) / np.cosh(s / np.sqrt(2)) ** 2, 0.0)
+    ef += pf
+    assert np.max(np.abs(f[0] - ef)) <= 1e-13
+    assert np.max(np.abs(p[0] - ep)) <= 1e-13
+    assert np.max(np.abs(ep)) > 0.1  # the walls move
