@@ -489,6 +489,7 @@ def fd_workloads(L, hbm):
     c = L.make_config(n, nfld=1, length=20.0, laplacian=L.LAP_FD7, precision=L.FP64, model=L.MODEL_PHI4)
     g = L.Lattice(c)
     g.init_vacuum(1000, [1.0], [0.0], [3.0], amp=1e-8, kcut_frac=0.5)
+    g.autotune(os.environ.get("LAT_TUNE_CACHE"))
     dt = 20.0 / n / 10
     g.symp(2, dt, 10)
     g.sync()
@@ -504,6 +505,7 @@ def fd_workloads(L, hbm):
     n = 512
     g = L.Lattice(bubble_config(L, n))
     init_bubbles(g, n)
+    g.autotune(os.environ.get("LAT_TUNE_CACHE"))
     dt = 0.25 / 10
     g.symp(2, dt, 3)
     g.sync()
@@ -521,6 +523,7 @@ def fd_workloads(L, hbm):
     bytes_kd = 120 * n ** 3  # phi (Kahan) 24 B + 6 u_ij and 6 pi_ij read+write 96 B
     ach = bytes_kd / (tkd / nkd * 1e-3) / 1e9 if nkd else None
     res["bubbles_512cube_fd27_gw_fp32"] = {"steps": K, "ms_per_step": ms / K, "value": n ** 3 * K / (ms * 1e-3),
+                                           "tuning": g.tuning(),
                                            "unit": UNIT, "kickdrift_avg_us": 1e3 * tkd / max(nkd, 1),
                                            "kickdrift_achieved_gbs": ach,
                                            "kickdrift_frac": ach / hbm if ach else None,
@@ -567,6 +570,8 @@ def run_fd_case(L, args, local):
     c.device = local
     g = L.Lattice(c)
     init_bubbles(g, n)
+    if not args.no_autotune:
+        g.autotune(os.environ.get("LAT_TUNE_CACHE"))
     dt = 0.25 / 10
     g.symp(2, dt, args.warmup)
     g.sync()
@@ -575,7 +580,7 @@ def run_fd_case(L, args, local):
     g.symp(2, dt, args.steps)
     g.mark(1)
     ms = g.mark_elapsed(0, 1)
-    print(json.dumps({"metric": f"site-updates/s @{n}^3 FD27 bubbles + GW, leapfrog, FP32-Kahan",
+    print(json.dumps({"metric": f"site-updates/s @{n}^3 FD27 bubbles + GW, leapfrog, FP32-Kahan", "tuning": g.tuning(),
                       "value": n ** 3 * args.steps / (ms * 1e-3), "unit": UNIT, "steps": args.steps,
                       "warmup": args.warmup, "ms_per_step": ms / args.steps,
                       "gpu_launches": g.launch_count() - l0}))

@@ -398,3 +398,78 @@ def test_boosted_bubbles_match_restatement(engine):
     assert np.max(np.abs(f[0] - ef)) <= 1e-13
     assert np.max(np.abs(p[0] - ep)) <= 1e-13
     assert np.max(np.abs(ep)) > 0.1  # the walls move
+
+
+@pytest.mark.parametrize("lap", [L.LAP_FD7, L.LAP_FD27, L.LAP_SPECTRAL])
+def test_non_cubic_lattices(engine, orc, lap):
+    """Uneven sides, one of them not a power of two (24: radix 3 in both FFTs)."""
+    shape = (32, 24, 16)
+    c = L.make_config(shape, nfld=2, length=12.0, laplacian=lap, background=L.BG_CONFORMAL,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g, o = pair(engine, orc, c)
+    same_start(g, o, amp=0.05)
+    for obj in (g, o):
+        obj.set_scale_factor(1.0, 0.0)
+        obj.calc_metric()
+        obj.symp(4, 0.02, 6)
+    compare_state(g, o)
+    assert np.allclose(g.scale_factor(), o.scale_factor(), rtol=1e-11, atol=0)
+    nb = 20
+    Sg, Wg = g.spectrum(L.SPEC_FLD, 1, L.SPEC_COUNT, nb)
+    So, Wo = o.spectrum(L.SPEC_FLD, 1, L.SPEC_COUNT, nb)
+    assert np.array_equal(Wg, Wo)
+    assert rel_err(Sg, So) <= 1e-10
+
+
+def test_spectral_defrost_conformal(engine, orc):
+    """DEFROST split order (metric, drift, kick) with the spectral kick and expansion."""
+    c = L.make_config(16, nfld=2, length=8.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                      split_order=L.SPLIT_DEFROST, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g, o = pair(engine, orc, c)
+    same_start(g, o, amp=0.05)
+    for obj in (g, o):
+        obj.set_scale_factor(1.0, 0.0)
+        obj.calc_metric()
+        obj.symp(6, 0.03, 4)
+    compare_state(g, o)
+    assert np.allclose(g.scale_factor(), o.scale_factor(), rtol=1e-11, atol=0)
+    assert np.allclose(g.time(), o.time(), rtol=0, atol=1e-14)
+
+
+def test_defrost_symp6_constant_and_symp8(engine, orc):
+    """The DEFROST tree's own symp6 constant is used with its split order, and its
+    symp8 (empty weights in the reference) is refused rather than run."""
+    c = bubble_fd27(16, gw=False, split=L.SPLIT_DEFROST)
+    g, o = pair(engine, orc, c)
+    same_start(g, o, mean=0.0, amp=0.3)
+    g.symp(6, 0.025, 3)
+    o.symp(6, 0.025, 3)
+    compare_state(g, o)
+    assert np.allclose(g.time(), o.time(), rtol=0, atol=1e-15)
+    with pytest.raises(engine.LatticeError):
+        g.symp(8, 0.025, 1)
+
+
+def test_fp32_kahan_tracks_fp64_oracle(engine, orc):
+    """The FP32-Kahan engine (both spectral paths) against the FP64 oracle."""
+    for impl in (L.SPEC_IMPL_CUFFT, L.SPEC_IMPL_SEPARABLE):
+        c = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                          precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0),
+                          spectral_impl=impl)
+        g = engine.Lattice(c)
+        c64 = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL,
+                            background=L.BG_CONFORMAL, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+        o = orc.Oracle(c64)
+        f, p = random_state((2, 32, 32, 64), seed=17, mean=1.0, amp=0.01)
+        for obj in (g, o):
+            obj.set_state(f, p)
+            obj.set_scale_factor(1.0, 0.0)
+            obj.calc_metric()
+            obj.symp(4, 0.02, 20)
+        gf, gp = g.get_state()
+        of, op = o.get_state()
+        # fluctuations of ~1e-2 around 1: compare the fluctuation, not the mean;
+        # FP32 rounding of fields near 1 is ~6e-8, i.e. ~1e-5 of the fluctuation
+        assert rel_err(gf - 1.0, of - 1.0) <= 1e-4, impl
+        assert rel_err(gp, op) <= 1e-4, impl
+        assert abs(g.scale_factor()[0] - o.scale_factor()[0]) <= 1e-8 * o.scale_factor()[0]
