@@ -333,6 +333,7 @@ typedef struct lat_net_s lat_net_t;
 enum lat_closure_units { LAT_UNITS_PROGRAM = 0, LAT_UNITS_CONFORMAL = 1 };
 int64_t lat_net_nparams(void);
 int lat_net_create(lat_net_t** out, int32_t device, uint64_t seed);
+/* refused (LAT_ERR_STATE) while the network is attached to a lattice */
 int lat_net_destroy(lat_net_t* n);
 /* flat FP32 parameters: W1[27][8][32] b1[32] W2[27][32][32] b2[32]
  * W3[27][32][8] b3[8]; tap = (dz+1)*9 + (dy+1)*3 + (dx+1) for the input

@@ -461,7 +461,7 @@ class Net:
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
-            _lib.lat_net_destroy(self._h)
+            _check(_lib.lat_net_destroy(self._h))
             self._h = C.c_void_p()
 
     def __del__(self):

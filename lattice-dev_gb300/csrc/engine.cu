@@ -827,6 +827,7 @@ int lat_destroy(lat_t* h) {
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_graphs(h);
+  if (h->cl_net) net::net_attach_ref(h->cl_net, -1);
   for (void* t : h->tw)
     if (t) cudaFree(t);
   {
@@ -1765,6 +1766,7 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
   CK(cudaStreamSynchronize(h->stream));
   free_graphs(h);
   if (!net) {
+    if (h->cl_net) net::net_attach_ref(h->cl_net, -1);
     h->cl_net = nullptr;
     return LAT_OK;
   }
@@ -1779,6 +1781,8 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
     CK(cudaMalloc(&h->cl_b.a2, (size_t)h->N * net::C_HID * 2));
     CK(cudaMalloc(&h->cl_b.out, (size_t)h->N * 2 * sizeof(float)));
   }
+  if (h->cl_net) net::net_attach_ref(h->cl_net, -1);
+  net::net_attach_ref(net, +1);
   h->cl_net = net;
   h->cl_every = every;
   h->cl_units = conformal(h) ? units : LAT_UNITS_PROGRAM;  // a = 1 in Minkowski

@@ -47,6 +47,7 @@ struct lat_net_s {
   int idx_cap = 0;
   int64_t launches = 0;
   int* err = nullptr;  // device error word of the tensor-memory convolutions (bounded waits)
+  int attached = 0;    // lattices this network is attached to (lat_closure_attach)
 };
 
 namespace {
@@ -257,6 +258,8 @@ int net_device(const lat_net_s* n) { return n->dev; }
 
 int* net_err(const lat_net_s* n) { return n->err; }
 
+void net_attach_ref(lat_net_s* n, int delta) { n->attached += delta; }
+
 }  // namespace net
 }  // namespace lat
 
@@ -327,6 +330,7 @@ int lat_net_create(lat_net_t** out, int32_t device, uint64_t seed) {
 
 int lat_net_destroy(lat_net_t* n) {
   if (!n) return LAT_OK;
+  if (n->attached > 0) return set_error(LAT_ERR_STATE, "network still attached to a lattice: detach it first");
   cudaSetDevice(n->dev);
   if (n->stream) cudaStreamSynchronize(n->stream);
   free_acts(n);

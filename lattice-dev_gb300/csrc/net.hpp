@@ -83,6 +83,7 @@ int infer(lat_net_s* n, const void* const ch[4], int fp64, int nx, int ny, int n
 void out_scale(const lat_net_s* n, double out[2]);
 int net_device(const lat_net_s* n);
 int* net_err(const lat_net_s* n);
+void net_attach_ref(lat_net_s* n, int delta);
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s);
 // 32 -> 32 channel layers on tcgen05 (k_conv_tc.cu): nx % 128 == 0, ny % 2 == 0

@@ -229,3 +229,17 @@ def test_closure_ablation_gain(engine):
     clos = np.mean([e["closure"]["pk_mean_rel_err"] for e in ev], axis=0)
     assert np.all(clos < 0.5 * plain), (plain, clos)
     ds.buf.close()
+
+
+def test_attached_network_cannot_be_destroyed(engine):
+    c = L.make_config((32, 16, 16), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, model=L.MODEL_PHI4_G2,
+                      model_params=(1.0, 2.0))
+    g = engine.Lattice(c)
+    net = engine.Net(seed=2)
+    g.attach_closure(net, 1, L.UNITS_PROGRAM)
+    with pytest.raises(engine.LatticeError) as ei:
+        net.close()
+    assert ei.value.code == 6  # LAT_ERR_STATE
+    g.attach_closure(None)
+    net.close()  # detached: freed
+    g.close()
