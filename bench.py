@@ -612,8 +612,8 @@ def conv_roofline(L, net, n, reps=10):
     ach = N * sum(v[0] for v in CONV_FLOPS_PER_SITE.values()) / tot / 1e12
     out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                        "peak_kind": kind + " dense bf16 (cuBLAS burst)",
-                       "note": "conv2 (32->32) on tcgen05.mma with TMEM accumulators when nx % 128 == 0, "
-                               "conv1 and conv3 on mma.sync; BF16 in, FP32 accumulate"}
+                       "note": "conv1 (4 padded to 8 -> 32) and conv2 (32->32) on tcgen05.mma with TMEM "
+                               "accumulators when nx % 128 == 0, conv3 (32->2) on mma.sync; BF16 in, FP32 accumulate"}
     return out
 
 

@@ -39,16 +39,26 @@ namespace {
 constexpr int TCX = 128, TCR = 2, ZC = 16;         // item: 128 x-sites, 2 y-rows, up to ZC z-planes
 constexpr int HXT = TCX + 2, HYT = TCR + 2;        // halo extents of one plane
 constexpr int CM_BYTES = 128;                      // one core matrix: 8 rows x 16 bytes
-constexpr int A_CHUNK = HXT * 16;                  // bytes between channel chunks (K direction) of A
-constexpr int A_YROW = 4 * A_CHUNK;                // bytes per halo y-row, all 4 chunks
-constexpr int A_PLANE = HYT * A_YROW;              // 33 280 bytes per halo plane
 constexpr int NSLOT = 4;                           // ring of halo planes
-constexpr int B_CHUNK = 32 * 16;                   // bytes between channel chunks of B
-constexpr int B_TAP = 4 * B_CHUNK;                 // 2 KB per tap
-constexpr int B_BYTES = 27 * B_TAP;                // 55 296
-constexpr int A_BYTES = NSLOT * A_PLANE;           // 133 120
+constexpr int B_CHUNK = 32 * 16;                   // bytes per 8-channel chunk of the 32 output rows of B
 constexpr int TMEM_COLS = 128;                     // 2 buffers x 2 rows x 32 fp32 columns
-constexpr int SMEM_TC = B_BYTES + A_BYTES + 64;    // + two mbarriers and the TMEM address
+
+// shared-memory geometry for CA input channels (32, or 8 = 4 padded)
+template <int CA>
+struct TcGeom {
+  static constexpr int CH = CA / 8;                        // 16-byte channel chunks per site
+  // CA 8 stages one more halo row: the partner rows of the third tap row
+  // (finite data, multiplied by zero weights)
+  static constexpr int HY = CA == 8 ? HYT + 1 : HYT;
+  static constexpr int A_CHUNK = HXT * 16;                 // bytes between channel chunks (K direction) of A
+  static constexpr int A_YROW = CH * A_CHUNK;              // bytes per halo y-row, all chunks
+  static constexpr int A_PLANE = HY * A_YROW;              // 33 280 (CA 32) or 10 400 (CA 8) bytes
+  static constexpr int A_BYTES = NSLOT * A_PLANE;
+  static constexpr int B_TAP = CH * B_CHUNK;               // 2 KB (CA 32) or 512 B (CA 8) per tap
+  // CA 8: a zero chunk after the 27 taps partners the third tap row of a plane
+  static constexpr int B_BYTES = 27 * B_TAP + (CA == 8 ? B_CHUNK : 0);
+  static constexpr int SMEM = B_BYTES + A_BYTES + 64;      // + two mbarriers and the TMEM address
+};
 constexpr int THREADS = 288;   // warps 0-7: copies and epilogue; warp 8: MMA issue
 constexpr int WORKERS = 256;
 constexpr uint32_t kSpinLimit = 1u << 20;
@@ -93,25 +103,31 @@ __device__ __forceinline__ float gelu_f(float z) { return gelu_t(z); }
 __device__ __forceinline__ float gelu_df(float z) { return gelu_t_d(z); }
 
 // copies of halo plane z (periodic) of an item into ring slot `slot`
+template <int CA>
 __device__ __forceinline__ void load_plane(uint32_t a_s, int slot, const __nv_bfloat16* src, const ConvArgs& a,
                                            int x0, int y0, int z) {
+  using G = TcGeom<CA>;
   z = z < 0 ? z + a.nz : (z >= a.nz ? z - a.nz : z);
-  const uint32_t base = a_s + slot * A_PLANE;
+  const uint32_t base = a_s + slot * G::A_PLANE;
   if (threadIdx.x >= WORKERS) return;  // the MMA warp issues no copies
-  for (int i = threadIdx.x; i < HYT * HXT * 4; i += WORKERS) {
-    const int c = i & 3;
-    const int s = i >> 2;
+  for (int i = threadIdx.x; i < G::HY * HXT * G::CH; i += WORKERS) {
+    const int c = i % G::CH;
+    const int s = i / G::CH;
     const int hx = s % HXT, hy = s / HXT;
     int x = x0 + hx - 1, y = y0 + hy - 1;
     x = x < 0 ? x + a.nx : (x >= a.nx ? x - a.nx : x);
     y = y < 0 ? y + a.ny : (y >= a.ny ? y - a.ny : y);
-    cp16(base + hy * A_YROW + c * A_CHUNK + hx * 16, src + (((int64_t)z * a.ny + y) * a.nx + x) * 32 + c * 8);
+    cp16(base + hy * G::A_YROW + c * G::A_CHUNK + hx * 16,
+         src + (((int64_t)z * a.ny + y) * a.nx + x) * CA + c * 8);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-template <int EPI, bool STORE_Z>
+template <int CA, int EPI, bool STORE_Z>
 __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* err) {
+  using G = TcGeom<CA>;
+  constexpr int A_CHUNK = G::A_CHUNK, A_YROW = G::A_YROW, A_PLANE = G::A_PLANE, B_TAP = G::B_TAP;
+  constexpr int B_BYTES = G::B_BYTES, A_BYTES = G::A_BYTES;
   extern __shared__ __align__(1024) unsigned char sm[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + B_BYTES + A_BYTES);  // [2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + B_BYTES + A_BYTES + 32);
@@ -132,10 +148,13 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   // weights [tap][co][ci] (global) -> [tap][ci chunk][co][8] (shared)
-  for (int i = tid; i < 27 * 32 * 4; i += THREADS) {
-    const int tap = i / 128, r = i % 128, n = r / 4, c = r % 4;
-    cp16(b_s + tap * B_TAP + c * B_CHUNK + n * 16, a.w + ((int64_t)tap * 32 + n) * 32 + c * 8);
+  for (int i = tid; i < 27 * 32 * G::CH; i += THREADS) {
+    const int tap = i / (32 * G::CH), r = i % (32 * G::CH), n = r / G::CH, c = r % G::CH;
+    cp16(b_s + tap * B_TAP + c * B_CHUNK + n * 16, a.w + ((int64_t)tap * 32 + n) * CA + c * 8);
   }
+  if constexpr (CA == 8)  // the zero chunk (made visible to the tensor core by the fence of step 0)
+    for (int i = tid; i < B_CHUNK / 16; i += THREADS)
+      *reinterpret_cast<uint4*>(sm + 27 * B_TAP + i * 16) = make_uint4(0, 0, 0, 0);
   asm volatile("cp.async.commit_group;\n" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
@@ -210,12 +229,12 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
     const int zc = (int)(rr / tiles_y);
     const int x0 = tx * TCX, y0 = ty * TCR, zA = zc * ZC;
     const int nzs = min(ZC, a.nz - zA);
-    const __nv_bfloat16* src = a.in + li * Nsite * 32;
+    const __nv_bfloat16* src = a.in + li * Nsite * CA;
     const int64_t lat_base = li * Nsite;
     // planes q = -1, 0, 1 of the item (q = z - zA) into slots (q + 1) & 3
-    load_plane(a_s, 0, src, a, x0, y0, zA - 1);
-    load_plane(a_s, 1, src, a, x0, y0, zA);
-    load_plane(a_s, 2, src, a, x0, y0, zA + 1);
+    load_plane<CA>(a_s, 0, src, a, x0, y0, zA - 1);
+    load_plane<CA>(a_s, 1, src, a, x0, y0, zA);
+    load_plane<CA>(a_s, 2, src, a, x0, y0, zA + 1);
 #pragma unroll 1
     for (int j = 0; j <= nzs; ++j) {
       const int buf = j & 1;
@@ -234,22 +253,42 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
           // descriptors are affine in the start address: one base per operand and
           // plane slot, compile-time offsets for the taps (the start-address field
           // never carries: shared addresses stay below 256 KB)
-          const uint64_t bd0 = mdesc(b_s, B_CHUNK, CM_BYTES);
 #pragma unroll
           for (int r = 0; r < TCR; ++r) {
             const uint32_t d = tmem + buf * 64 + r * 32;
-            uint64_t ad0[3];
+            if constexpr (CA == 32) {
+              const uint64_t bd0 = mdesc(b_s, B_CHUNK, CM_BYTES);
+              uint64_t ad0[3];
 #pragma unroll
-            for (int dz = 0; dz < 3; ++dz)
-              ad0[dz] = mdesc(a_s + ((j + dz) & 3) * A_PLANE + r * A_YROW, A_CHUNK, CM_BYTES);
+              for (int dz = 0; dz < 3; ++dz)
+                ad0[dz] = mdesc(a_s + ((j + dz) & 3) * A_PLANE + r * A_YROW, A_CHUNK, CM_BYTES);
 #pragma unroll
-            for (int tap = 0; tap < 27; ++tap) {
-              const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+              for (int tap = 0; tap < 27; ++tap) {
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
 #pragma unroll
-              for (int k = 0; k < 2; ++k) {
-                const uint64_t ad = ad0[dz] + (uint64_t)((dy * A_YROW + dx * 16 + 2 * k * A_CHUNK) >> 4);
-                const uint64_t bd = bd0 + (uint64_t)((tap * B_TAP + 2 * k * B_CHUNK) >> 4);
-                mma_bf16(d, ad, bd, (tap | k) ? 1u : 0u);
+                for (int k = 0; k < 2; ++k) {
+                  const uint64_t ad = ad0[dz] + (uint64_t)((dy * A_YROW + dx * 16 + 2 * k * A_CHUNK) >> 4);
+                  const uint64_t bd = bd0 + (uint64_t)((tap * B_TAP + 2 * k * B_CHUNK) >> 4);
+                  mma_bf16(d, ad, bd, (tap | k) ? 1u : 0u);
+                }
+              }
+            } else {
+              // 8 channels per tap: one K16 step takes the taps (dy 0, dx) and
+              // (dy 1, dx) of a plane, the second 8-channel core matrix of A and
+              // B one halo row and three taps further (LBO); the taps (dy 2, dx)
+              // pair with the row below (finite data) times the zero chunk of B
+#pragma unroll
+              for (int dz = 0; dz < 3; ++dz) {
+                const uint32_t abase = a_s + ((j + dz) & 3) * A_PLANE + r * A_YROW;
+#pragma unroll
+                for (int p = 0; p < 6; ++p) {
+                  const int dx = p % 3, dy = p < 3 ? 0 : 2;
+                  const int tap0 = dz * 9 + dy * 3 + dx;
+                  const uint32_t lbo_b = p < 3 ? (uint32_t)(3 * B_TAP) : (uint32_t)((27 - tap0) * B_TAP);
+                  const uint64_t ad = mdesc(abase + dy * A_YROW + dx * 16, A_YROW, CM_BYTES);
+                  const uint64_t bd = mdesc(b_s + tap0 * B_TAP, lbo_b, CM_BYTES);
+                  mma_bf16(d, ad, bd, (dz | p) ? 1u : 0u);
+                }
               }
             }
           }
@@ -279,7 +318,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
           phase[pb] ^= 1u;
           pending[pb] = 0;
           // the slot of plane j-2 is free: prefetch plane j+2 behind the epilogue
-          if (j + 2 <= nzs) load_plane(a_s, (j + 3) & 3, src, a, x0, y0, zA + j + 2);
+          if (j + 2 <= nzs) load_plane<CA>(a_s, (j + 3) & 3, src, a, x0, y0, zA + j + 2);
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           epilogue(pb, lat_base, x0, y0, zA + j - 1);
         }
@@ -292,7 +331,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
         }
       } else if (2 <= nzs) {
         // j == 0: slot 3 is free; prefetch plane 2
-        load_plane(a_s, 3, src, a, x0, y0, zA + 2);
+        load_plane<CA>(a_s, 3, src, a, x0, y0, zA + 2);
       }
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -321,23 +360,30 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int* er
 }  // namespace
 
 bool conv_tc_ok(int ca, int cb, int epi, int nx, int ny) {
-  return ca == 32 && cb == 32 && epi != EPI_LINEAR && nx % TCX == 0 && ny % TCR == 0;
+  if (nx % TCX || ny % TCR || cb != 32) return false;
+  return (ca == 32 && epi != EPI_LINEAR) || (ca == 8 && epi == EPI_GELU);
 }
 
-int conv_tc(const ConvArgs& a, int epi, int nsm, int* err, cudaStream_t s) {
+int conv_tc(const ConvArgs& a, int ca, int epi, int nsm, int* err, cudaStream_t s) {
   const bool sz = a.zout != nullptr;
-  auto go = [&](auto kern) -> int {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);
+  auto go = [&](auto kern, int smem) -> int {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_fail(e, "tcgen05 conv smem attribute");
     const int64_t nitems = (int64_t)(a.nx / TCX) * (a.ny / TCR) * ((a.nz + ZC - 1) / ZC) * a.nlat;
     const unsigned grid = (unsigned)std::min<int64_t>(nitems, (int64_t)nsm);
-    kern<<<grid, THREADS, SMEM_TC, s>>>(a, err);
+    kern<<<grid, THREADS, smem, s>>>(a, err);
     if (g_launch_counter) ++*g_launch_counter;
     e = cudaGetLastError();
     return e == cudaSuccess ? LAT_OK : cuda_fail(e, "tcgen05 conv launch");
   };
-  if (epi == EPI_GELU) return sz ? go(conv_tc_kernel<EPI_GELU, true>) : go(conv_tc_kernel<EPI_GELU, false>);
-  return go(conv_tc_kernel<EPI_BWD, false>);
+  if (ca == 8) {
+    constexpr int sm8 = TcGeom<8>::SMEM;
+    return sz ? go(conv_tc_kernel<8, EPI_GELU, true>, sm8) : go(conv_tc_kernel<8, EPI_GELU, false>, sm8);
+  }
+  constexpr int sm32 = TcGeom<32>::SMEM;
+  if (epi == EPI_GELU)
+    return sz ? go(conv_tc_kernel<32, EPI_GELU, true>, sm32) : go(conv_tc_kernel<32, EPI_GELU, false>, sm32);
+  return go(conv_tc_kernel<32, EPI_BWD, false>, sm32);
 }
 
 }  // namespace net

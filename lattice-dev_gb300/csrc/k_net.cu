@@ -515,7 +515,7 @@ int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s) {
     const char* v = getenv("LAT_NO_TCGEN05");
     return v && v[0] && v[0] != '0';
   }();
-  if (!no_tc && a.err && conv_tc_ok(ca, cb, epi, a.nx, a.ny)) return conv_tc(a, epi, nsm, a.err, s);
+  if (!no_tc && a.err && conv_tc_ok(ca, cb, epi, a.nx, a.ny)) return conv_tc(a, ca, epi, nsm, a.err, s);
   const bool sz = a.zout != nullptr;
   if (ca == 8 && cb == 32 && epi == EPI_GELU) return sz ? conv_go<8, 32, EPI_GELU, true>(a, nsm, s)
                                                         : conv_go<8, 32, EPI_GELU, false>(a, nsm, s);

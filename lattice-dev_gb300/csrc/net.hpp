@@ -86,9 +86,10 @@ int* net_err(const lat_net_s* n);
 void net_attach_ref(lat_net_s* n, int delta);
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s);
-// 32 -> 32 channel layers on tcgen05 (k_conv_tc.cu): nx % 128 == 0, ny % 2 == 0
+// layers with 32 output channels on tcgen05 (k_conv_tc.cu): 32 -> 32 (forward and
+// backward data) and the 8-channel (4 padded) input layer; nx % 128 == 0, ny % 2 == 0
 bool conv_tc_ok(int ca, int cb, int epi, int nx, int ny);
-int conv_tc(const ConvArgs& a, int epi, int nsm, int* err, cudaStream_t s);
+int conv_tc(const ConvArgs& a, int ca, int epi, int nsm, int* err, cudaStream_t s);
 int wgrad_blocks(int nsm);
 int wgrad(const WgradArgs& a, int cx, int cd, int nblk, float* dW, float* db, cudaStream_t s);
 int pack(const PackArgs& a, int fp64, int nsm, cudaStream_t s);
