@@ -599,6 +599,22 @@ int copy_aos(lat_s* h, double* host, int lo, int hi, bool to_device) {
   return LAT_OK;
 }
 
+// Device address of a host array the GPU reads and writes in place (pinned
+// and mapped: cudaHostAlloc, lat_host_alloc, cudaHostRegister), else null.
+// Unpadded Fortran arrays at such addresses are converted by one kernel that
+// reads or writes host memory over the CPU-GPU link, with no staging copy;
+// LAT_NO_DIRECT_HOST=1 forces the staged copies.
+double* mapped_host(const void* host) {
+  if (getenv_flag("LAT_NO_DIRECT_HOST")) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<double*>(at.devicePointer);
+}
+
 int read_scalars(lat_s* h, DevScalars* out) {
   CK(cudaMemcpyAsync(out, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -1023,15 +1039,20 @@ int lat_upload(lat_t* h, const double* fld, int32_t fld_lo, int32_t fld_hi, cons
   ApiGuard g(h);
   RET(ensure_stage(h, (size_t)h->nf * h->N));
   if (fld) {
-    RET(copy_aos(h, const_cast<double*>(fld), fld_lo, fld_hi, true));
-    RET(launch_aos2soa(h->stage, h->nf, h->N, h->prec, h->fld[h->cur], h->fldc, h->stream));
+    const double* d = (fld_lo == 0 && fld_hi == 0) ? mapped_host(fld) : nullptr;
+    if (!d) {
+      RET(copy_aos(h, const_cast<double*>(fld), fld_lo, fld_hi, true));
+      d = h->stage;
+    }
+    RET(launch_aos2soa(d, h->nf, h->N, h->prec, h->fld[h->cur], h->fldc, h->stream));
   }
   if (fldp) {
-    RET(copy_aos(h, const_cast<double*>(fldp), fldp_lo, fldp_hi, true));
-    RET(launch_aos2soa(h->stage, h->nf, h->N, h->prec, h->fldp, nullptr, h->stream));
-    if (h->prec == LAT_FP32_KAHAN) {
-      // momenta carry no compensation; the kernel wrote c only when given one
+    const double* d = (fldp_lo == 0 && fldp_hi == 0) ? mapped_host(fldp) : nullptr;
+    if (!d) {
+      RET(copy_aos(h, const_cast<double*>(fldp), fldp_lo, fldp_hi, true));
+      d = h->stage;
     }
+    RET(launch_aos2soa(d, h->nf, h->N, h->prec, h->fldp, nullptr, h->stream));  // momenta: no compensation
   }
   CK(cudaStreamSynchronize(h->stream));
   return LAT_OK;
@@ -1044,12 +1065,14 @@ int lat_download(lat_t* h, double* fld, int32_t fld_lo, int32_t fld_hi, double* 
   ApiGuard g(h);
   RET(ensure_stage(h, (size_t)h->nf * h->N));
   if (fld) {
-    RET(launch_soa2aos(h->fld[h->cur], h->fldc, h->nf, h->N, h->prec, h->stage, h->stream));
-    RET(copy_aos(h, fld, fld_lo, fld_hi, false));
+    double* d = (fld_lo == 0 && fld_hi == 0) ? mapped_host(fld) : nullptr;
+    RET(launch_soa2aos(h->fld[h->cur], h->fldc, h->nf, h->N, h->prec, d ? d : h->stage, h->stream));
+    if (!d) RET(copy_aos(h, fld, fld_lo, fld_hi, false));
   }
   if (fldp) {
-    RET(launch_soa2aos(h->fldp, nullptr, h->nf, h->N, h->prec, h->stage, h->stream));
-    RET(copy_aos(h, fldp, fldp_lo, fldp_hi, false));
+    double* d = (fldp_lo == 0 && fldp_hi == 0) ? mapped_host(fldp) : nullptr;
+    RET(launch_soa2aos(h->fldp, nullptr, h->nf, h->N, h->prec, d ? d : h->stage, h->stream));
+    if (!d) RET(copy_aos(h, fldp, fldp_lo, fldp_hi, false));
   }
   CK(cudaStreamSynchronize(h->stream));
   return LAT_OK;

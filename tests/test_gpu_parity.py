@@ -240,6 +240,46 @@ def test_fortran_layout_padding(engine):
     assert np.all(back[mask] == -7.0)  # ghost sites untouched
 
 
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32_KAHAN])
+def test_pinned_host_arrays_direct(engine, prec):
+    """Unpadded pinned arrays are converted in place over the CPU-GPU link;
+    the result must equal the staged copy of the same pageable arrays."""
+    import ctypes
+
+    c = phi4_fd7(16, prec)
+    c.nfld = 2
+    c.model = L.MODEL_PHI4_G2
+    n, nf = 16, 2
+    rng = np.random.default_rng(11)
+    fld = rng.standard_normal((n, n, n, nf))
+    fldp = rng.standard_normal((n, n, n, nf))
+    nbytes = fld.nbytes
+    ptrs = [engine.host_alloc(nbytes) for _ in range(2)]
+    try:
+        pin = [np.ctypeslib.as_array((ctypes.c_double * fld.size).from_address(p)).reshape(fld.shape) for p in ptrs]
+        pin[0][...] = fld
+        pin[1][...] = fldp
+        a, b = engine.Lattice(c), engine.Lattice(c)
+        a.upload_fortran(pin[0], 0, 0, pin[1], 0, 0)
+        b.upload_fortran(fld, 0, 0, fldp, 0, 0)
+        fa, pa = a.get_state()
+        fb, pb = b.get_state()
+        assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
+        for g in (a, b):
+            g.symp(2, 0.05, 3)
+        pin[0][...] = -1.0
+        pin[1][...] = -1.0
+        a.download_fortran(pin[0], 0, 0, pin[1], 0, 0)
+        back, backp = np.empty_like(fld), np.empty_like(fldp)
+        b.download_fortran(back, 0, 0, backp, 0, 0)
+        assert np.array_equal(pin[0], back) and np.array_equal(pin[1], backp)
+        a.close()
+        b.close()
+    finally:
+        for p in ptrs:
+            engine.host_free(p)
+
+
 def test_checkpoint_roundtrip(engine, tmp_path):
     c = two_field_spectral(16, conformal=True)
     g = engine.Lattice(c)
