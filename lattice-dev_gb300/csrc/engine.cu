@@ -126,6 +126,7 @@ struct lat_s {
 
   bool sep_ok = false;            // separable spectral passes available for these sizes
   bool sep = false;               // and in use
+  bool sep_stream = true;         // streamed passes where available (LAT_SEP_CLASSIC=1: off)
   void* tw[3] = {nullptr, nullptr, nullptr};  // W_N^j per axis, field precision
 
   int fd_ty = 8, fd_zc = 32;
@@ -424,6 +425,8 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
                        : (axis == 1 ? (int64_t)h->nx * h->nz / pairs : (int64_t)h->nx * h->ny / pairs);
   a.sc = h->sc;
   a.rb = red(h);
+  a.nsm = h->nsm;
+  a.stream = h->sep_stream ? 1 : 0;
   int st;
   switch (n) {
     case 16: st = launch_sep_16(a, h->prec, axis, h->stream); break;
@@ -988,6 +991,7 @@ int lat_create(lat_t** out, const lat_config* cfg) {
     if (cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !h->sep_ok)
       return bail(set_error(LAT_ERR_UNSUPPORTED, "separable spectral passes need power-of-two sides 16..512"));
     h->sep = h->sep_ok && cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !getenv_flag("LAT_NO_SEPARABLE");
+    h->sep_stream = !getenv_flag("LAT_SEP_CLASSIC");
     if (h->sep_ok) {
       if ((st = alloc(&h->fld[1], fb))) return bail(st);
       if (h->prec == LAT_FP32_KAHAN && (st = alloc(&h->fldc_alt, fb))) return bail(st);

@@ -83,6 +83,8 @@ struct SepArgs {
   double Nd;
   int conf;
   int64_t nlines;   // complex lines of this pass
+  int nsm;          // SMs of the device (grid of the streamed passes)
+  int stream;       // 1: streamed passes where available (k_sep_stream.cuh)
   DevScalars* sc;
   RedBuf rb;
 };

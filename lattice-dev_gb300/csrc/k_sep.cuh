@@ -173,17 +173,19 @@ __device__ __forceinline__ void d2_line(R (&re)[Split<N>::Q], R (&im)[Split<N>::
       ui[g][tt] = z.y;
     }
     dft<P, false, R>(ur[g], ui[g]);
+    R gpart = R(0);  // this thread's P modes, folded into `ge` once
 #pragma unroll
     for (int kp = 0; kp < P; ++kp) {
       const int k = kq + Q * kp;
       const int f = k <= N / 2 ? k : k - N;
       const R f2 = (R)(f * f) * dk2;  // (f dk)^2
       const R zr = ur[g][kp], zi = ui[g][kp];
-      ge.add(f2 * (zr * zr + zi * zi) * (R)(1.0 / N));
+      gpart += f2 * (zr * zr + zi * zi);
       const R h = -f2 * (R)(1.0 / N);
       ur[g][kp] = zr * h;
       ui[g][kp] = zi * h;
     }
+    ge.add(gpart * (R)(1.0 / N));
     dft<P, true, R>(ur[g], ui[g]);
   }
   __syncthreads();
