@@ -404,11 +404,16 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
   a.phi = h->fld[h->cur];
   a.phic = h->fldc;
   a.pi = h->fldp;
-  a.lap = axis == 2 ? h->lap_alt : h->lap;
   a.phi_out = h->fld[1 - h->cur];
   a.phic_out = h->fldc_alt;
   a.pi_out = h->fldp_alt;
-  a.lap_out = axis == 0 ? h->lap : h->lap_alt;
+  if (h->sep_stream) {  // lap holds zs, written by X; every pass updates the momenta
+    a.lap = h->lap;
+    a.lap_out = h->lap;
+  } else {
+    a.lap = axis == 2 ? h->lap_alt : h->lap;
+    a.lap_out = axis == 0 ? h->lap : h->lap_alt;
+  }
   a.twN = h->tw[axis];
   if (!h->sep_ok || !a.twN || !a.phi || !a.phi_out || !a.pi || !a.pi_out || !a.lap || !a.lap_out ||
       (h->prec == LAT_FP32_KAHAN && (!a.phic || !a.phic_out)))
@@ -441,9 +446,8 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
   if (axis == 0) {  // drifted fields now live in the second buffers
     h->cur = 1 - h->cur;
     std::swap(h->fldc, h->fldc_alt);
-  } else if (axis == 2) {  // kicked momenta
-    std::swap(h->fldp, h->fldp_alt);
   }
+  if (axis == 2 || h->sep_stream) std::swap(h->fldp, h->fldp_alt);  // (partly) kicked momenta
   return LAT_OK;
 }
 
@@ -479,9 +483,16 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
     return LAT_ERR_UNSUPPORTED;
   }
   double pending = lead;
+  if (h->sep_stream && conf && !grp.empty()) {  // sum pi^2 for the first pass X
+    Timed t(h, LAT_K_OTHER);
+    RET(launch_pi2_sum(h->fldp, (int64_t)h->nf * h->N, h->sc, red(h), 2 * h->nsm, h->stream));
+  }
   for (const Grp& g : grp) {
-    RET(sep_pass(h, 0, 0.0, 0.0, pending));
-    RET(sep_pass(h, 1, 0.0, 0.0, 0.0));
+    // the streamed pass X starts the kick, so it takes the group's kick and
+    // grav-kinetic weights too
+    if (h->sep_stream) RET(sep_pass(h, 0, g.hk, g.hg, pending));
+    else RET(sep_pass(h, 0, 0.0, 0.0, pending));
+    RET(sep_pass(h, 1, h->sep_stream ? g.hk : 0.0, h->sep_stream ? g.hg : 0.0, 0.0));
     RET(sep_pass(h, 2, g.hk, g.hg, 0.0));
     pending = g.hd;
   }
@@ -991,7 +1002,15 @@ int lat_create(lat_t** out, const lat_config* cfg) {
     if (cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !h->sep_ok)
       return bail(set_error(LAT_ERR_UNSUPPORTED, "separable spectral passes need power-of-two sides 16..512"));
     h->sep = h->sep_ok && cfg->spectral_impl == LAT_SPEC_IMPL_SEPARABLE && !getenv_flag("LAT_NO_SEPARABLE");
-    h->sep_stream = !getenv_flag("LAT_SEP_CLASSIC");
+    // two FP32 fields on lines of 128 or 256 points whose passes all form
+    // whole tiles: the streamed passes (LAT_SEP_CLASSIC=1 keeps the others)
+    auto stream_lines = [](int n, int axis) {
+      return n == 128 ? sep_stream_lines_128(axis) : (n == 256 ? sep_stream_lines_256(axis) : 0);
+    };
+    const int lx = stream_lines(h->nx, 0), ly = stream_lines(h->ny, 1), lz = stream_lines(h->nz, 2);
+    h->sep_stream = h->sep_ok && h->prec == LAT_FP32_KAHAN && h->nf == 2 && lx && ly && lz &&
+                    ((int64_t)h->ny * h->nz) % lx == 0 && h->nx % ly == 0 && h->nx % lz == 0 &&
+                    !getenv_flag("LAT_SEP_CLASSIC");
     if (h->sep_ok) {
       if ((st = alloc(&h->fld[1], fb))) return bail(st);
       if (h->prec == LAT_FP32_KAHAN && (st = alloc(&h->fldc_alt, fb))) return bail(st);

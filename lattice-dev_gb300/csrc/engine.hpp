@@ -84,7 +84,7 @@ struct SepArgs {
   int conf;
   int64_t nlines;   // complex lines of this pass
   int nsm;          // SMs of the device (grid of the streamed passes)
-  int stream;       // 1: streamed passes where available (k_sep_stream.cuh)
+  int stream;       // 1: the streamed passes of k_sep_stream.cuh (other buffer roles)
   DevScalars* sc;
   RedBuf rb;
 };
@@ -94,6 +94,9 @@ int launch_sep_64(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_128(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_256(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_512(const SepArgs& a, int precision, int axis, cudaStream_t s);
+int sep_stream_lines_128(int axis);  // lines per tile of the streamed passes (k_sep_stream.cuh)
+int sep_stream_lines_256(int axis);
+int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s);
 int sep_columns_16(int precision, int nf);
 int sep_columns_32(int precision, int nf);
 int sep_columns_64(int precision, int nf);

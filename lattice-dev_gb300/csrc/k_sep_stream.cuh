@@ -1,23 +1,28 @@
 // k_sep_stream.cuh -- streamed separable spectral passes for two FP32 fields.
 //
-// Same arithmetic as sep_kernel (k_sep.cuh: passes X, Y, Z of the spectral
-// Laplacian of laplacian_3d, Pseudospec/openmp_dev/fftw_mod.f90:177-207, with
-// the drift and kick of hamiltonian_conformal.f90:92-174 fused in), organised
-// for latency hiding instead of occupancy:
+// The spectral Laplacian of laplacian_3d (Pseudospec/openmp_dev/fftw_mod.f90:
+// 177-207) is the sum of one-dimensional second derivatives along x, y and z
+// (k_sep.cuh).  For two FP32 fields on lines of 128 or 256 points the engine
+// runs the three passes of a drift + kick in this form:
 //
-// * one persistent block of 256 threads per SM walks its share of the tiles
-//   (LINES complex lines each);
-// * every input of a tile is copied into shared memory by cp.async, issued
-//   one or two tiles ahead, so HBM reads stay in flight while the block runs
-//   the line transforms of the current tile;
-// * a tile's early inputs (the transform input; in X also the momenta of the
-//   drift) and late inputs (Y: lap; Z: lap and pi, used after the transform)
-//   are separate loads in a ring of slots, and the slot whose early inputs
-//   were just read serves as the transform's transpose scratch before it is
-//   refilled.
+//   pass X: drift of phi (Kahan), z = (phi - shift) - c written as the FP32
+//           array zs, pi += ck d2x(z)                       [PE, GEx, means]
+//   pass Y: pi += ck d2y(zs)                                 [GEy]
+//   pass Z: pi += ck d2z(zs) - cv V'(zs + shift)             [GEz, sum pi^2]
 //
-// The ring keeps a fixed number of cp.async groups in flight (an empty group
-// is committed past the last tile), so every wait is wait_group(SLOTS - 1).
+// with ck = hk a1^2, cv = hk a1^4, a1 = a - hg ysclp / 6 after the drift's
+// ysclp += hd sum(pi^2)/N / a^3 (hamiltonian_conformal.f90:86-174).  The
+// momenta accumulate the kick pass by pass, so no Laplacian array is kept:
+// per field and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
+// needs ck before it has seen all momenta, so sum pi^2 comes from the pass Z
+// of the previous kick (or one reduction before the first pass X of a call).
+//
+// Blocks are persistent.  A block reads the inputs of its tile from shared
+// memory into registers, refills the slot with the next tile's inputs by
+// cp.async at once, and runs the line transforms in a separate scratch, so the
+// next tile's HBM reads are in flight during the transforms.  X: 128-thread
+// blocks, 3 per SM; Y, Z: 256-thread blocks, 2 per SM, with a second slot for
+// the momenta, which are needed only after the transform.
 #pragma once
 #include "k_sep.cuh"
 
@@ -31,30 +36,30 @@ template <int K> __device__ __forceinline__ void cp_wait_keep() {
 template <int AXIS, int N>
 struct STile {
   static constexpr int P = Split<N>::P, Q = Split<N>::Q;
-  static constexpr int THREADS = 256, LINES = THREADS / P;
+  static constexpr int THREADS = AXIS == 0 ? 128 : 256, LINES = THREADS / P;
+  static constexpr int MINB = AXIS == 0 ? 3 : 2;  // blocks per SM
   // X: one staged row per line (padded by P floats so the 32/P lines of a
   // warp start in different banks); Y, Z: one row of LINES x-columns per
   // position along the line
   static constexpr int RS = AXIS == 0 ? N + P : LINES;
   static constexpr int ROWS = AXIS == 0 ? LINES : N;
-  static constexpr int ARR = ROWS * RS;  // floats per staged array
-  static constexpr int N_EARLY = AXIS == 0 ? 6 : 4;  // X: phi, c, pi of both fields; Y, Z: phi, c
-  static constexpr int N_LATE = AXIS == 0 ? 0 : (AXIS == 1 ? 2 : 4);  // Y: lap; Z: lap, pi
-  static constexpr int LPT = N_LATE ? 2 : 1;  // loads per tile
-  static constexpr int SLOTS = LPT == 1 ? 2 : 3;
-  static constexpr int SLOT = N_EARLY * ARR;  // floats per slot
+  static constexpr int ARR = ROWS * RS;               // floats per staged array
+  static constexpr int N_EARLY = AXIS == 0 ? 6 : 2;   // X: phi, c, pi of both fields; Y, Z: zs
+  static constexpr int N_LATE = AXIS == 0 ? 0 : 2;    // Y, Z: pi of both fields
   static constexpr int LSTRIDE = Tile<float, 2, AXIS, N>::LSTRIDE;
-  static constexpr int SMEM = SLOTS * SLOT * 4 + N * 8;
-  static_assert(LINES * LSTRIDE * 8 <= SLOT * 4, "transform scratch must fit in a slot");
-  static_assert(RS % 4 == 0 && (AXIS != 0 || N % 4 == 0), "staged rows must hold whole 16-byte copies");
-  static_assert(SMEM <= 220 * 1024, "ring must fit in shared memory");
+  static constexpr int E_OFF = 0, L_OFF = N_EARLY * ARR, S_OFF = L_OFF + N_LATE * ARR;  // floats
+  static constexpr int TW_OFF = S_OFF + LINES * LSTRIDE * 2;
+  static constexpr int SMEM = TW_OFF * 4 + N * 8;
+  // MINB blocks, each with its dynamic and static (reduction) shared memory
+  // and the 1 KB the SM reserves per block, fit in 228 KB
+  static_assert(MINB * (SMEM + 1300 + 1024) <= 228 * 1024, "blocks per SM must fit in shared memory");
+  static_assert(RS % 4 == 0 && N % 4 == 0, "staged rows must hold whole 16-byte copies");
 };
 
-// Copy one load of tile `tile` (part 0: early inputs, 1: late inputs) into a
-// slot with 16-byte cp.async copies spread over the block.  Every array of a
-// load is 64 Q copies; thread tid always copies chunk tid % CPR of rows
-// tid / CPR + j * (THREADS / CPR), so its addresses are one base per array
-// plus compile-time steps.
+// Copy the early (part 0) or late (part 1) inputs of tile `tile` into the
+// slot `dst` with 16-byte cp.async copies.  Thread tid always copies chunk
+// tid % CPR of rows tid / CPR + j * (THREADS / CPR), so its addresses are one
+// base per array plus compile-time steps.
 template <int AXIS, int N>
 __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t tile, int part, int tid) {
   using T = STile<AXIS, N>;
@@ -76,230 +81,264 @@ __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t
   }
   const int64_t jstep = RPJ * stride;
   float* d0 = dst + row0 * T::RS + ch * 4;
-  // arrays: X [field][phi, c, pi]; early [field][phi, c]; late Y [field][lap], late Z [field][lap, pi]
-  constexpr int NA = AXIS == 0 ? 6 : (T::N_EARLY > T::N_LATE ? T::N_EARLY : T::N_LATE);
-  const int narr = AXIS == 0 ? 6 : (part == 0 ? T::N_EARLY : T::N_LATE);
-  const int per_f = AXIS == 0 ? 3 : (part == 0 ? 2 : T::N_LATE / 2);
+  // arrays: X [field][phi, c, pi]; Y, Z early [field] zs, late [field] pi
+  constexpr int NA = AXIS == 0 ? 6 : 2;
+  constexpr int PERF = AXIS == 0 ? 3 : 1;
 #pragma unroll
   for (int arr = 0; arr < NA; ++arr) {
-    if (arr < narr) {
-      const int f = arr / per_f, k = arr % per_f;
-      const void* sp = AXIS == 0 ? (k == 0 ? a.phi : (k == 1 ? a.phic : a.pi))
-                                 : (part == 0 ? (k == 0 ? a.phi : a.phic) : (k == 0 ? a.lap : a.pi));
-      const float* src = static_cast<const float*>(sp) + f * Ns + src0;
-      float* d = d0 + arr * T::ARR;
+    const int f = arr / PERF, k = arr % PERF;
+    const void* sp = AXIS == 0 ? (k == 0 ? a.phi : (k == 1 ? a.phic : a.pi)) : (part == 0 ? a.lap : a.pi);
+    const float* src = static_cast<const float*>(sp) + f * Ns + src0;
+    float* d = d0 + arr * T::ARR;
 #pragma unroll
-      for (int j = 0; j < STEPS; ++j) cp16(d + j * RPJ * T::RS, src + j * jstep);
-    }
+    for (int j = 0; j < STEPS; ++j) cp16(d + j * RPJ * T::RS, src + j * jstep);
   }
 }
 
-template <int AXIS, int N>
-__global__ void __launch_bounds__(256, 1) sep_stream_kernel(const __grid_constant__ SepArgs a) {
-  using T = STile<AXIS, N>;
-  constexpr int P = T::P, Q = T::Q, LINES = T::LINES, S = T::SLOTS, LPT = T::LPT;
+// Pass X: drift, zs and the x part of the kick.
+template <int N>
+__global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
+    sep_stream_x(const __grid_constant__ SepArgs a) {
+  using T = STile<0, N>;
+  constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* slots = reinterpret_cast<float*>(smraw);
-  float2* twN = reinterpret_cast<float2*>(slots + S * T::SLOT);
-  const int tid = threadIdx.x;
-  const int t = AXIS == 0 ? tid % P : tid / LINES;
-  const int li = AXIS == 0 ? tid / P : tid % LINES;
+  float* sm = reinterpret_cast<float*>(smraw);
+  float* es = sm + T::E_OFF;
+  float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
+  float2* twN = reinterpret_cast<float2*>(sm + T::TW_OFF);
+  const int tid = threadIdx.x, t = tid % P, li = tid / P;
   const int64_t ntiles = a.nlines / LINES;
   const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  auto issue = [&](int64_t k) {
-    const int64_t j = k / LPT;
-    if (j < my) stage_load<AXIS, N>(a, slots + (k % S) * T::SLOT, (int64_t)blockIdx.x + j * gridDim.x,
-                                    (int)(k % LPT), tid);
-    cp_commit();
-  };
+  if (my > 0) stage_load<0, N>(a, es, blockIdx.x, 0, tid);
+  cp_commit();
+  for (int j = tid; j < N; j += T::THREADS) twN[j] = static_cast<const float2*>(a.twN)[j];
+
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  float* __restrict__ phi_o = static_cast<float*>(a.phi_out);
+  float* __restrict__ phic_o = static_cast<float*>(a.phic_out);
+  float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
+  float* __restrict__ zs_o = static_cast<float*>(a.lap_out);
+  const DevScalars* sc = a.sc;
+  const double shAd = __ldcg(&sc->mean[0]), shBd = __ldcg(&sc->mean[1]);
+  const float shA = (float)shAd, shB = (float)shBd;
+  const float dk2 = (float)a.dk2;
+  const bool drift = a.hd != 0.0;
+  double a0 = 1.0, ap0 = 0.0, ke = 0.0;
+  float cd = (float)a.hd, ck = (float)a.hk;
+  if (a.conf) {
+    a0 = __ldcg(&sc->a);
+    ke = __ldcg(&sc->ke_cur);
+    ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
+    const double a1 = a0 - a.hg * ap0 / 6.0;                     // Hamiltonian_grav_kinetic
+    cd = (float)(a.hd / (a0 * a0));
+    ck = (float)(a.hk * a1 * a1);
+  }
+  KSum ge, pe, mA, mB;
+  for (int64_t j = 0; j < my; ++j) {
+    const int64_t l = ((int64_t)blockIdx.x + j * gridDim.x) * LINES + li;
+    const int64_t offA = l * a.nx, offB = Nsite + offA;
+    cp_wait_keep<0>();
+    __syncthreads();
+    float vr[Q], vi[Q], pA[Q], pB[Q];
+    float pes = 0.f, mAs = 0.f, mBs = 0.f;  // this line's sums, folded into KSum once
+    const float* row = es + li * T::RS;
 #pragma unroll
-  for (int k = 0; k < S; ++k) issue(k);
+    for (int q = 0; q < Q; ++q) {
+      const int pos = t + P * q;
+      float fA = row[pos], cA = row[T::ARR + pos];
+      float fB = row[3 * T::ARR + pos], cB = row[4 * T::ARR + pos];
+      pA[q] = row[2 * T::ARR + pos];
+      pB[q] = row[5 * T::ARR + pos];
+      if (drift) {
+        kahan_add(fA, cA, cd * pA[q]);
+        kahan_add(fB, cB, cd * pB[q]);
+      }
+      phi_o[offA + pos] = fA;
+      phi_o[offB + pos] = fB;
+      phic_o[offA + pos] = cA;
+      phic_o[offB + pos] = cB;
+      if (a.conf) {
+        float ff[2] = {fA, fB};
+        pes += model_v<float, 2>(a.model, ff);
+      }
+      mAs += fA;
+      mBs += fB;
+      vr[q] = (fA - shA) - cA;
+      vi[q] = (fB - shB) - cB;
+      zs_o[offA + pos] = vr[q];
+      zs_o[offB + pos] = vi[q];
+    }
+    pe.add(pes);
+    mA.add(mAs);
+    mB.add(mBs);
+    __syncthreads();  // the slot is free: stage the next tile
+    if (j + 1 < my) stage_load<0, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
+    cp_commit();
+    d2_line<N, float, float2>(vr, vi, t, scr + li * T::LSTRIDE, twN, dk2, ge);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int pos = t + P * q;
+      pi_o[offA + pos] = pA[q] + ck * vr[q];
+      pi_o[offB + pos] = pB[q] + ck * vi[q];
+    }
+  }
+  cp_wait_all();
+  double vals[4] = {pe.val(), ge.val(), mA.val(), mB.val()}, tot[4];
+  if (grid_reduce<4>(vals, a.rb, tot)) {
+    DevScalars* w = a.sc;
+    if (a.conf) {
+      w->ap = ap0;
+      w->pe = tot[0] / a.Nd;
+      if (drift) w->ke2 = ke;
+    }
+    w->gsum[0] = tot[1];
+    w->zsh[0] = shAd;
+    w->zsh[1] = shBd;
+    w->mean[0] = tot[2] / a.Nd;
+    w->mean[1] = tot[3] / a.Nd;
+    if (bad(tot[0]) || bad(tot[1])) w->err |= 1u;
+  }
+}
+
+// Passes Y (AXIS 1) and Z (AXIS 2): the y part of the kick; the z part with
+// the potential force, which completes the kick and its ysclp update.
+template <int AXIS, int N>
+__global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
+    sep_stream_yz(const __grid_constant__ SepArgs a) {
+  using T = STile<AXIS, N>;
+  constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* sm = reinterpret_cast<float*>(smraw);
+  float* es = sm + T::E_OFF;
+  float* ls = sm + T::L_OFF;
+  float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
+  float2* twN = reinterpret_cast<float2*>(sm + T::TW_OFF);
+  const int tid = threadIdx.x, t = tid / LINES, li = tid % LINES;
+  const int64_t ntiles = a.nlines / LINES;
+  const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  if (my > 0) stage_load<AXIS, N>(a, es, blockIdx.x, 0, tid);
+  cp_commit();
+  if (my > 0) stage_load<AXIS, N>(a, ls, blockIdx.x, 1, tid);
+  cp_commit();
   for (int j = tid; j < N; j += T::THREADS) twN[j] = static_cast<const float2*>(a.twN)[j];
 
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
   const int64_t plane = (int64_t)a.nx * a.ny;
-  float* __restrict__ phi_o = static_cast<float*>(a.phi_out);
-  float* __restrict__ phic_o = static_cast<float*>(a.phic_out);
+  const int64_t st = AXIS == 1 ? a.nx : plane;
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
-  float* __restrict__ lap_o = static_cast<float*>(a.lap_out);
   const DevScalars* sc = a.sc;
-  const float shA = (float)__ldcg(&sc->mean[0]);
-  const float shB = (float)__ldcg(&sc->mean[1]);
   const float dk2 = (float)a.dk2;
-  KSum ge, ke, pe, mA, mB;
-  // X: drift coefficient; Z: kick coefficients after Hamiltonian_grav_kinetic
+  const float zshA = (float)__ldcg(&sc->zsh[0]), zshB = (float)__ldcg(&sc->zsh[1]);
   double a0 = 1.0, ap0 = 0.0, a1 = 1.0;
-  float cd = (float)a.hd, ck = (float)a.hk, cv = (float)a.hk;
-  const bool drift = a.hd != 0.0;
+  float ck = (float)a.hk, cv = (float)a.hk;
   if (a.conf) {
     a0 = __ldcg(&sc->a);
     ap0 = __ldcg(&sc->ap);
-    if (AXIS == 0) cd = (float)(a.hd / (a0 * a0));
-    if (AXIS == 2) {
-      a1 = a0 - a.hg * ap0 / 6.0;
-      ck = (float)(a.hk * a1 * a1);
-      cv = (float)(a.hk * a1 * a1 * a1 * a1);
-    }
+    a1 = a0 - a.hg * ap0 / 6.0;  // Hamiltonian_grav_kinetic before the kick
+    ck = (float)(a.hk * a1 * a1);
+    cv = (float)(a.hk * a1 * a1 * a1 * a1);
   }
-
+  KSum ge, ke;
   for (int64_t j = 0; j < my; ++j) {
-    const int64_t k = j * LPT;
     const int64_t l = ((int64_t)blockIdx.x + j * gridDim.x) * LINES + li;
-    float* es = slots + (k % S) * T::SLOT;
-    cp_wait_keep<S - 1>();
+    const int64_t x = l % a.nx, o = l / a.nx;
+    const int64_t offA = (AXIS == 1 ? o * plane : o * a.nx) + x, offB = Nsite + offA;
+    cp_wait_keep<1>();  // zs of this tile (its momenta may still be in flight)
     __syncthreads();
     float vr[Q], vi[Q];
     float hA[AXIS == 2 ? Q : 1], hB[AXIS == 2 ? Q : 1];
-    int64_t offA, st;
-    if constexpr (AXIS == 0) {
-      offA = l * a.nx;
-      st = 1;
-    } else {
-      const int64_t x = l % a.nx, o = l / a.nx;
-      offA = (AXIS == 1 ? o * plane : o * a.nx) + x;
-      st = AXIS == 1 ? a.nx : plane;
-    }
-    const int64_t offB = Nsite + offA;
-    auto at = [&](const float* sl, int arr, int pos) -> float {
-      return AXIS == 0 ? sl[arr * T::ARR + li * T::RS + pos] : sl[arr * T::ARR + pos * T::RS + li];
-    };
-    float kes = 0.f, pes = 0.f, mAs = 0.f, mBs = 0.f;  // this line's sums, folded into KSum once
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
-      if constexpr (AXIS == 0) {
-        float fA = at(es, 0, pos), cA = at(es, 1, pos);
-        float fB = at(es, 3, pos), cB = at(es, 4, pos);
-        if (drift) {
-          const float pA = at(es, 2, pos), pB = at(es, 5, pos);
-          kahan_add(fA, cA, cd * pA);
-          kahan_add(fB, cB, cd * pB);
-          if (a.conf) kes += pA * pA + pB * pB;
-        }
-        phi_o[offA + pos] = fA;
-        phi_o[offB + pos] = fB;
-        phic_o[offA + pos] = cA;
-        phic_o[offB + pos] = cB;
-        if (a.conf) {
-          float ff[2] = {fA, fB};
-          pes += model_v<float, 2>(a.model, ff);
-        }
-        mAs += fA;
-        mBs += fB;
-        vr[q] = (fA - shA) - cA;
-        vi[q] = (fB - shB) - cB;
-      } else {
-        const float fA = at(es, 0, pos), cA = at(es, 1, pos);
-        const float fB = at(es, 2, pos), cB = at(es, 3, pos);
-        vr[q] = (fA - shA) - cA;
-        vi[q] = (fB - shB) - cB;
-        if constexpr (AXIS == 2) {
-          hA[q] = fA - cA;
-          hB[q] = fB - cB;
-        }
+      vr[q] = es[pos * T::RS + li];
+      vi[q] = es[T::ARR + pos * T::RS + li];
+      if constexpr (AXIS == 2) {
+        hA[q] = vr[q] + zshA;  // phi - c
+        hB[q] = vi[q] + zshB;
       }
     }
-    if constexpr (AXIS == 0) {
-      ke.add(kes);
-      pe.add(pes);
-      mA.add(mAs);
-      mB.add(mBs);
-    }
-    __syncthreads();  // the slot becomes the transform scratch
-    d2_line<N, float, float2>(vr, vi, t, reinterpret_cast<float2*>(es) + li * T::LSTRIDE, twN, dk2, ge);
     __syncthreads();
-    issue(k + S);  // refill the slot
-    if constexpr (AXIS == 0) {
+    if (j + 1 < my) stage_load<AXIS, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
+    cp_commit();
+    d2_line<N, float, float2>(vr, vi, t, scr + li * T::LSTRIDE, twN, dk2, ge);
+    cp_wait_keep<1>();  // the momenta of this tile
+    __syncthreads();
+    float kes = 0.f;
 #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int pos = t + P * q;
-        lap_o[offA + pos] = vr[q];
-        lap_o[offB + pos] = vi[q];
+    for (int q = 0; q < Q; ++q) {
+      const int pos = t + P * q;
+      const int64_t sA = offA + (int64_t)pos * st, sB = offB + (int64_t)pos * st;
+      float pA = ls[pos * T::RS + li], pB = ls[T::ARR + pos * T::RS + li];
+      if constexpr (AXIS == 1) {
+        pA = pA + ck * vr[q];
+        pB = pB + ck * vi[q];
+      } else {
+        float ff[2] = {hA[q], hB[q]}, dv[2];
+        model_dv<float, 2>(a.model, ff, dv);
+        pA = pA + (ck * vr[q] - cv * dv[0]);
+        pB = pB + (ck * vi[q] - cv * dv[1]);
+        kes += pA * pA + pB * pB;
       }
-    } else {
-      const float* ls = slots + ((k + 1) % S) * T::SLOT;
-      cp_wait_keep<S - 1>();
-      __syncthreads();
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int pos = t + P * q;
-        const int64_t sA = offA + (int64_t)pos * st, sB = offB + (int64_t)pos * st;
-        if constexpr (AXIS == 1) {
-          lap_o[sA] = at(ls, 0, pos) + vr[q];
-          lap_o[sB] = at(ls, 1, pos) + vi[q];
-        } else {
-          const float lA = at(ls, 0, pos) + vr[q], lB = at(ls, 2, pos) + vi[q];
-          float ff[2] = {hA[q], hB[q]}, dv[2];
-          model_dv<float, 2>(a.model, ff, dv);
-          pi_o[sA] = at(ls, 1, pos) + (ck * lA - cv * dv[0]);
-          pi_o[sB] = at(ls, 3, pos) + (ck * lB - cv * dv[1]);
-        }
-      }
-      __syncthreads();
-      issue(k + 1 + S);
+      pi_o[sA] = pA;
+      pi_o[sB] = pB;
     }
+    if (AXIS == 2) ke.add(kes);
+    __syncthreads();
+    if (j + 1 < my) stage_load<AXIS, N>(a, ls, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 1, tid);
+    cp_commit();
   }
   cp_wait_all();
-
-  if constexpr (AXIS == 0) {
-    double vals[5] = {ke.val(), pe.val(), ge.val(), mA.val(), mB.val()}, tot[5];
-    if (grid_reduce<5>(vals, a.rb, tot)) {
-      DevScalars* w = a.sc;
-      if (a.conf) {
-        w->ap = w->ap + a.hd * (tot[0] / a.Nd) / (a0 * a0 * a0);
-        w->pe = tot[1] / a.Nd;
-        if (drift) w->ke2 = tot[0];
-      }
-      w->gsum[0] = tot[2];
-      w->mean[0] = tot[3] / a.Nd;
-      w->mean[1] = tot[4] / a.Nd;
-      if (bad(tot[0]) || bad(tot[1]) || bad(tot[2])) w->err |= 1u;
-    }
-  } else if constexpr (AXIS == 1) {
-    if (a.conf) {
-      double vals[1] = {ge.val()}, tot[1];
-      if (grid_reduce<1>(vals, a.rb, tot)) a.sc->gsum[1] = tot[0];
-    }
+  if (!a.conf) return;
+  if constexpr (AXIS == 1) {
+    double vals[1] = {ge.val()}, tot[1];
+    if (grid_reduce<1>(vals, a.rb, tot)) a.sc->gsum[1] = tot[0];
   } else {
-    if (a.conf) {
-      double vals[1] = {ge.val()}, tot[1];
-      if (grid_reduce<1>(vals, a.rb, tot)) {
-        DevScalars* w = a.sc;
-        const double GE2 = (w->gsum[0] + w->gsum[1] + tot[0]) / (a1 * a1) / a.Nd;
-        const double ap1 = ap0 - a1 * a1 * a1 * (GE2 + 4.0 * w->pe) * a.hk;
-        w->gsum[2] = tot[0];
-        w->ap = ap1;
-        w->a = a1 - a.hg * ap1 / 6.0;
-        if (bad(GE2)) w->err |= 1u;
-      }
+    double vals[2] = {ge.val(), ke.val()}, tot[2];
+    if (grid_reduce<2>(vals, a.rb, tot)) {
+      DevScalars* w = a.sc;
+      const double GE2 = (w->gsum[0] + w->gsum[1] + tot[0]) / (a1 * a1) / a.Nd;
+      const double ap1 = ap0 - a1 * a1 * a1 * (GE2 + 4.0 * w->pe) * a.hk;  // the kick's ysclp update
+      w->gsum[2] = tot[0];
+      w->ap = ap1;
+      w->a = a1 - a.hg * ap1 / 6.0;  // second Hamiltonian_grav_kinetic
+      w->ke_cur = tot[1];            // sum pi^2 for the next pass X
+      if (bad(GE2) || bad(tot[1])) w->err |= 1u;
     }
   }
 }
 
-// Launch of the streamed pass: one block per SM (fewer when there are fewer
-// tiles).  Returns LAT_ERR_UNSUPPORTED (nothing launched) when the lines do
-// not form whole tiles.
-template <int AXIS, int N>
-int sep_stream_go(const SepArgs& a, cudaStream_t s) {
-  using T = STile<AXIS, N>;
-  if (a.nf != 2 || a.nlines % T::LINES || (AXIS != 0 && a.nx % T::LINES)) return LAT_ERR_UNSUPPORTED;
-  auto k = sep_stream_kernel<AXIS, N>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM);
+template <typename K>
+int stream_launch(K k, int smem, int threads, int minb, int64_t ntiles, const SepArgs& a, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return cuda_fail(e, "streamed separable pass smem attribute");
-  const int64_t ntiles = a.nlines / T::LINES;
-  const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
-  k<<<grid, T::THREADS, T::SMEM, s>>>(a);
+  const int64_t cap = (int64_t)minb * a.nsm;
+  const int grid = (int)(ntiles < cap ? ntiles : cap);
+  k<<<grid, threads, smem, s>>>(a);
   if (g_launch_counter) ++*g_launch_counter;
   e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "streamed separable pass launch");
 }
 
+// Lines per block tile of the streamed pass along `axis` (the host checks
+// that every pass of a lattice forms whole tiles before choosing them).
+template <int N>
+int stream_lines(int axis) {
+  return axis == 0 ? STile<0, N>::LINES : (axis == 1 ? STile<1, N>::LINES : STile<2, N>::LINES);
+}
+
 template <int N>
 int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
+  const int lines = stream_lines<N>(axis);
+  if (a.nf != 2 || a.nlines % lines || (axis != 0 && a.nx % lines))
+    return set_error(LAT_ERR_STATE, "streamed separable pass: lines do not form whole tiles");
+  const int64_t ntiles = a.nlines / lines;
   switch (axis) {
-    case 0: return sep_stream_go<0, N>(a, s);
-    case 1: return sep_stream_go<1, N>(a, s);
-    default: return sep_stream_go<2, N>(a, s);
+    case 0: return stream_launch(sep_stream_x<N>, STile<0, N>::SMEM, STile<0, N>::THREADS, STile<0, N>::MINB,
+                                 ntiles, a, s);
+    case 1: return stream_launch(sep_stream_yz<1, N>, STile<1, N>::SMEM, STile<1, N>::THREADS, STile<1, N>::MINB,
+                                 ntiles, a, s);
+    default: return stream_launch(sep_stream_yz<2, N>, STile<2, N>::SMEM, STile<2, N>::THREADS, STile<2, N>::MINB,
+                                  ntiles, a, s);
   }
 }
 

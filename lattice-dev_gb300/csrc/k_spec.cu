@@ -261,6 +261,20 @@ __global__ void __launch_bounds__(256) kmul_kernel(KmulArgs a) {
 
 __global__ void grav_kernel(DevScalars* sc, double h) { sc->a = sc->a - h * sc->ap / 6.0; }
 
+// sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur
+__global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb) {
+  KSum s;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 v = __ldcs(pi + i);
+    s.add((v.x * v.x + v.y * v.y) + (v.z * v.z + v.w * v.w));
+  }
+  double vals[1] = {s.val()}, tot[1];
+  if (grid_reduce<1>(vals, rb, tot)) {
+    sc->ke_cur = tot[0];
+    if (bad(tot[0])) sc->err |= 1u;
+  }
+}
+
 }  // namespace
 
 int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s) {
@@ -275,6 +289,14 @@ int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
   if (g_launch_counter) ++*g_launch_counter;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "kmul launch");
+}
+
+int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s) {
+  if (n % 4) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
+  pi2_kernel<<<grid, 256, 0, s>>>(static_cast<const float4*>(pi), n / 4, sc, rb);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "momenta sum launch");
 }
 
 int launch_grav(DevScalars* sc, double h, cudaStream_t s) {
