@@ -315,17 +315,22 @@ def diagnostics(L, g, args, dt, ms_step):
     for v in cls.values():
         v["share"] = v["ms"] / tot
     out["kernel_classes"] = cls
-    # algorithmic bytes per launch of the engine kernels (2 fields)
-    # per launch, two FP32 fields: X r phi,c,pi w phi,c,lap; Y r phi,c,lap w lap; Z r phi,c,lap,pi w pi
-    bytes_per = {"kickdrift": 2 * 28 * N, "kmul": 2 * 2 * 8 * (n // 2 + 1) * n * n,
-                 "drift": 2 * 20 * N, "sep_x": 2 * 24 * N, "sep_y": 2 * 16 * N, "sep_z": 2 * 20 * N}
+    # algorithmic bytes per launch of the engine kernels, two FP32 fields.
+    # Streamed separable passes: X r phi,c,pi w phi,c,zs,pi; Y r zs,pi w pi; Z r zs,pi w pi.
+    # Other separable passes: X r phi,c,pi w phi,c,lap; Y r phi,c,lap w lap; Z r phi,c,lap,pi w pi.
+    streamed = g.sep_streamed()
+    sep_b = (28, 12, 12) if streamed else (24, 16, 20)
+    bytes_per = {"kickdrift": 2 * 28 * N, "kmul": 2 * 2 * 8 * (n // 2 + 1) * n * n, "drift": 2 * 20 * N,
+                 "sep_x": 2 * sep_b[0] * N, "sep_y": 2 * sep_b[1] * N, "sep_z": 2 * sep_b[2] * N}
     own = {k: v for k, v in cls.items() if k in bytes_per}
     if own:
         dom = max(own, key=lambda k: own[k]["ms"])
         avg_s = own[dom]["avg_us"] * 1e-6
         ach = bytes_per[dom] / avg_s / 1e9
         out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                           "frac": ach / hbm, "traffic": ncu_traffic(dom),
+                           "frac": ach / hbm,
+                           "traffic": ncu_traffic(dom, "spectral256_2f_fp32_streamed" if streamed and
+                                                  dom.startswith("sep") else "spectral256_2f_fp32"),
                            "algorithmic_bytes_per_launch": bytes_per[dom],
                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                                              "same workload (profiles/dram_traffic_256cube.txt)"}
@@ -346,10 +351,11 @@ def diagnostics(L, g, args, dt, ms_step):
     out["spectral_paths"] = paths
     # each path's whole step against its own byte model: the cuFFT path moves
     # 3 kicks x (2 fields x (r2c + c2r: N reals + M complex each) + 28 B/site/field);
-    # the separable path 3 kicks x 2 fields x (24 + 16 + 20) B/site
+    # the streamed separable passes 3 kicks x 2 fields x (28 + 12 + 12) B/site
+    # (the others 24 + 16 + 20)
     M = (n // 2 + 1) * n * n
     fft_bytes = 3 * (2 * (2 * 4 * N + 2 * 8 * M) + 2 * 28 * N)
-    sep_bytes = 3 * 2 * 60 * N
+    sep_bytes = 3 * 2 * (52 if streamed else 60) * N
     out["step_roofline"] = {
         "cufft": {"bytes_per_step": fft_bytes, "ms_per_step": paths["cufft"]["ms_per_step"],
                   "achieved_gbs": fft_bytes / (paths["cufft"]["ms_per_step"] * 1e-3) / 1e9},

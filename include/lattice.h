@@ -421,6 +421,10 @@ int lat_autotune(lat_t* h, const char* cache_path);
 /* The choice in use: FD tile tx, ty, zchunk; pointwise block threads, blocks
  * per SM; spectral path (LAT_SPEC_IMPL_CUFFT or LAT_SPEC_IMPL_SEPARABLE). */
 int lat_tuning_get(const lat_t* h, int32_t out[6]);
+/* 1 when the handle's separable passes are the streamed kind (two FP32
+ * fields, every side 128 or 256: the kick accumulates in the momenta pass by
+ * pass and no Laplacian array is kept), else 0. */
+int lat_sep_streamed(const lat_t* h, int32_t* on);
 
 #ifdef __cplusplus
 }

@@ -118,7 +118,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_timing_reset": ([P], I), "lat_mark": ([P, I], I), "lat_mark_elapsed": ([P, I, I, dp], I), "lat_launch_count": ([P, C.POINTER(I64)], I),
         "lat_device_ptr": ([P, I, C.POINTER(P)], I), "lat_host_alloc": ([C.POINTER(P), C.c_size_t], I),
         "lat_host_free": ([P], I), "lat_autotune": ([P, C.c_char_p], I),
-        "lat_tuning_get": ([P, C.POINTER(I)], I),
+        "lat_tuning_get": ([P, C.POINTER(I)], I), "lat_sep_streamed": ([P, C.POINTER(I)], I),
         "lat_dev_alloc": ([I, C.POINTER(P), C.c_size_t], I), "lat_dev_free": ([P], I),
         "lat_memcpy": ([P, P, C.c_size_t, I], I),
         "lat_net_nparams": ([], I64), "lat_net_create": ([C.POINTER(P), I, U64], I), "lat_net_destroy": ([P], I),
@@ -390,6 +390,11 @@ class Lattice:
         out = (C.c_int32 * 6)()
         _check(_lib.lat_tuning_get(self._h, out))
         return list(out)
+
+    def sep_streamed(self) -> bool:
+        on = C.c_int32()
+        _check(_lib.lat_sep_streamed(self._h, C.byref(on)))
+        return bool(on.value)
 
     # output files in the reference's column layouts
     def write_energy_line(self, path, time: float) -> None:

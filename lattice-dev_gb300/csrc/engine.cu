@@ -1958,6 +1958,12 @@ int lat_write_spectrum_block(lat_t* h, const char* path) {
   return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);
 }
 
+int lat_sep_streamed(const lat_t* h, int32_t* on) {
+  if (!h || !on) return set_error(LAT_ERR_ARG, "null argument");
+  *on = h->sep_ok && h->sep_stream ? 1 : 0;
+  return LAT_OK;
+}
+
 int lat_tuning_get(const lat_t* h, int32_t out[6]) {
   if (!h || !out) return set_error(LAT_ERR_ARG, "null argument");
   out[0] = 32; out[1] = h->fd_ty; out[2] = h->fd_zc; out[3] = h->pw_block; out[4] = h->pw_grid / h->nsm;

@@ -21,8 +21,9 @@
 // memory into registers, refills the slot with the next tile's inputs by
 // cp.async at once, and runs the line transforms in a separate scratch, so the
 // next tile's HBM reads are in flight during the transforms.  X: 128-thread
-// blocks, 3 per SM; Y, Z: 256-thread blocks, 2 per SM, with a second slot for
-// the momenta, which are needed only after the transform.
+// blocks, 3 per SM, in which every warp stages and transforms its own lines
+// with warp barriers only; Y, Z: 256-thread blocks, 2 per SM, with a second
+// slot for the momenta, which are needed only after the transform.
 #pragma once
 #include "k_sep.cuh"
 
@@ -31,6 +32,91 @@ namespace sep {
 
 template <int K> __device__ __forceinline__ void cp_wait_keep() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
+}
+
+// Spectral second derivative of one complex line, as d2_line (k_sep.cuh) but
+// with per-block tables instead of per-point index arithmetic:
+// tf[kq * P + t] = W_N^{t kq} and ti[mp * Q + kq] = W_N^{mp kq} (the same
+// table when P == Q), fk[k] = (f dk)^2 for wavenumber index k.  Every table
+// read is the thread's base plus a compile-time offset.  WARP: the P threads
+// of every line sit in one warp, so the transposes need only warp barriers.
+template <int N, bool WARP, typename Acc>
+__device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im)[Split<N>::Q], int t, float2* sl,
+                                            const float2* tf, const float2* ti, const float* fk, Acc& ge) {
+  constexpr int P = Split<N>::P, Q = Split<N>::Q, G = Q / P, S = P + 1;
+  auto sync = [] {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+  };
+  dft<Q, false, float>(re, im);
+  const float2* tft = tf + t;
+#pragma unroll
+  for (int kq = 0; kq < Q; ++kq) {
+    const float2 w = tft[kq * P];
+    const float xr = re[kq], xi = im[kq];
+    sl[kq * S + t] = make_float2(xr * w.x - xi * w.y, xr * w.y + xi * w.x);
+  }
+  sync();
+  float ur[G][P], ui[G][P];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const int kq = t + g * P;
+#pragma unroll
+    for (int tt = 0; tt < P; ++tt) {
+      const float2 z = sl[kq * S + tt];
+      ur[g][tt] = z.x;
+      ui[g][tt] = z.y;
+    }
+    dft<P, false, float>(ur[g], ui[g]);
+    const float* fkk = fk + kq;  // k = kq + Q kp
+    float gpart = 0.f;
+#pragma unroll
+    for (int kp = 0; kp < P; ++kp) {
+      const float f2 = fkk[Q * kp];
+      const float zr = ur[g][kp], zi = ui[g][kp];
+      gpart += f2 * (zr * zr + zi * zi);
+      const float h = -f2 * (1.0f / N);
+      ur[g][kp] = zr * h;
+      ui[g][kp] = zi * h;
+    }
+    ge.add(gpart * (1.0f / N));
+    dft<P, true, float>(ur[g], ui[g]);
+  }
+  sync();
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const int kq = t + g * P;
+    const float2* tik = ti + kq;
+#pragma unroll
+    for (int mp = 0; mp < P; ++mp) {
+      const float2 w = tik[mp * Q];
+      const float xr = ur[g][mp], xi = ui[g][mp];
+      sl[kq * S + mp] = make_float2(xr * w.x + xi * w.y, xi * w.x - xr * w.y);  // times conj(W_N^{mp kq})
+    }
+  }
+  sync();
+#pragma unroll
+  for (int kq = 0; kq < Q; ++kq) {
+    const float2 z = sl[kq * S + t];
+    re[kq] = z.x;
+    im[kq] = z.y;
+  }
+  dft<Q, true, float>(re, im);
+}
+
+// Build the tables of d2_line_tab from W_N^j (global) in shared memory.
+template <int N>
+__device__ __forceinline__ void build_tables(const float2* twN, float dk2, float2* tf, float2* ti, float* fk, int tid,
+                                             int nthreads) {
+  constexpr int P = Split<N>::P, Q = Split<N>::Q;
+  for (int j = tid; j < P * Q; j += nthreads) {
+    tf[j] = twN[((j % P) * (j / P)) & (N - 1)];
+    if (P != Q) ti[j] = twN[((j / Q) * (j % Q)) & (N - 1)];
+  }
+  for (int k = tid; k < N; k += nthreads) {
+    const int f = k <= N / 2 ? k : k - N;
+    fk[k] = (float)(f * f) * dk2;
+  }
 }
 
 template <int AXIS, int N>
@@ -48,8 +134,10 @@ struct STile {
   static constexpr int N_LATE = AXIS == 0 ? 0 : 2;    // Y, Z: pi of both fields
   static constexpr int LSTRIDE = Tile<float, 2, AXIS, N>::LSTRIDE;
   static constexpr int E_OFF = 0, L_OFF = N_EARLY * ARR, S_OFF = L_OFF + N_LATE * ARR;  // floats
-  static constexpr int TW_OFF = S_OFF + LINES * LSTRIDE * 2;
-  static constexpr int SMEM = TW_OFF * 4 + N * 8;
+  static constexpr int TF_OFF = S_OFF + LINES * LSTRIDE * 2;  // twiddle tables W_N^{t kq}, W_N^{mp kq}
+  static constexpr int TI_OFF = P == Q ? TF_OFF : TF_OFF + 2 * N;
+  static constexpr int FK_OFF = TI_OFF + 2 * N;                   // (f dk)^2
+  static constexpr int SMEM = (FK_OFF + N) * 4;
   // MINB blocks, each with its dynamic and static (reduction) shared memory
   // and the 1 KB the SM reserves per block, fit in 228 KB
   static_assert(MINB * (SMEM + 1300 + 1024) <= 228 * 1024, "blocks per SM must fit in shared memory");
@@ -95,6 +183,30 @@ __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t
   }
 }
 
+// Pass X staging by one warp: the rows of its own 32/P lines of tile `tile`
+// (6 arrays: [field][phi, c, pi]), so the warp waits only for its own copies.
+template <int N>
+__device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64_t tile, int warp, int lane) {
+  using T = STile<0, N>;
+  constexpr int LPW = 32 / T::P, CPR = N / 4;  // lines per warp, 16-byte chunks per row
+  static_assert(CPR % 32 == 0 || 32 % CPR == 0, "a row is whole lanes");
+  const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
+  const int64_t r0 = tile * T::LINES + warp * LPW;  // first line (row) of the warp
+  float* d0 = dst + warp * LPW * T::RS;
+#pragma unroll
+  for (int arr = 0; arr < 6; ++arr) {
+    const int f = arr / 3, k = arr % 3;
+    const void* sp = k == 0 ? a.phi : (k == 1 ? a.phic : a.pi);
+    const float* src = static_cast<const float*>(sp) + f * Ns + r0 * a.nx;
+#pragma unroll
+    for (int r = 0; r < LPW; ++r) {
+#pragma unroll
+      for (int c = lane; c < CPR; c += 32)
+        cp16(d0 + arr * T::ARR + r * T::RS + c * 4, src + (int64_t)r * a.nx + c * 4);
+    }
+  }
+}
+
 // Pass X: drift, zs and the x part of the kick.
 template <int N>
 __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
@@ -105,13 +217,16 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   float* sm = reinterpret_cast<float*>(smraw);
   float* es = sm + T::E_OFF;
   float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
-  float2* twN = reinterpret_cast<float2*>(sm + T::TW_OFF);
-  const int tid = threadIdx.x, t = tid % P, li = tid / P;
+  float2* tf = reinterpret_cast<float2*>(sm + T::TF_OFF);
+  float2* ti = reinterpret_cast<float2*>(sm + T::TI_OFF);
+  float* fk = sm + T::FK_OFF;
+  const int tid = threadIdx.x, t = tid % P, li = tid / P, warp = tid / 32, lane = tid % 32;
   const int64_t ntiles = a.nlines / LINES;
   const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (my > 0) stage_load<0, N>(a, es, blockIdx.x, 0, tid);
+  if (my > 0) stage_rows_x<N>(a, es, blockIdx.x, warp, lane);
   cp_commit();
-  for (int j = tid; j < N; j += T::THREADS) twN[j] = static_cast<const float2*>(a.twN)[j];
+  build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+  __syncthreads();  // tables; from here on every warp runs its own lines
 
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
   float* __restrict__ phi_o = static_cast<float*>(a.phi_out);
@@ -121,7 +236,6 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   const DevScalars* sc = a.sc;
   const double shAd = __ldcg(&sc->mean[0]), shBd = __ldcg(&sc->mean[1]);
   const float shA = (float)shAd, shB = (float)shBd;
-  const float dk2 = (float)a.dk2;
   const bool drift = a.hd != 0.0;
   double a0 = 1.0, ap0 = 0.0, ke = 0.0;
   float cd = (float)a.hd, ck = (float)a.hk;
@@ -138,7 +252,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     const int64_t l = ((int64_t)blockIdx.x + j * gridDim.x) * LINES + li;
     const int64_t offA = l * a.nx, offB = Nsite + offA;
     cp_wait_keep<0>();
-    __syncthreads();
+    __syncwarp();
     float vr[Q], vi[Q], pA[Q], pB[Q];
     float pes = 0.f, mAs = 0.f, mBs = 0.f;  // this line's sums, folded into KSum once
     const float* row = es + li * T::RS;
@@ -171,10 +285,10 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     pe.add(pes);
     mA.add(mAs);
     mB.add(mBs);
-    __syncthreads();  // the slot is free: stage the next tile
-    if (j + 1 < my) stage_load<0, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
+    __syncwarp();  // the warp's rows are free: stage its rows of the next tile
+    if (j + 1 < my) stage_rows_x<N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, warp, lane);
     cp_commit();
-    d2_line<N, float, float2>(vr, vi, t, scr + li * T::LSTRIDE, twN, dk2, ge);
+    d2_line_tab<N, true>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
@@ -212,7 +326,9 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   float* es = sm + T::E_OFF;
   float* ls = sm + T::L_OFF;
   float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
-  float2* twN = reinterpret_cast<float2*>(sm + T::TW_OFF);
+  float2* tf = reinterpret_cast<float2*>(sm + T::TF_OFF);
+  float2* ti = reinterpret_cast<float2*>(sm + T::TI_OFF);
+  float* fk = sm + T::FK_OFF;
   const int tid = threadIdx.x, t = tid / LINES, li = tid % LINES;
   const int64_t ntiles = a.nlines / LINES;
   const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -220,14 +336,13 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   cp_commit();
   if (my > 0) stage_load<AXIS, N>(a, ls, blockIdx.x, 1, tid);
   cp_commit();
-  for (int j = tid; j < N; j += T::THREADS) twN[j] = static_cast<const float2*>(a.twN)[j];
+  build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
 
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
   const int64_t plane = (int64_t)a.nx * a.ny;
   const int64_t st = AXIS == 1 ? a.nx : plane;
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   const DevScalars* sc = a.sc;
-  const float dk2 = (float)a.dk2;
   const float zshA = (float)__ldcg(&sc->zsh[0]), zshB = (float)__ldcg(&sc->zsh[1]);
   double a0 = 1.0, ap0 = 0.0, a1 = 1.0;
   float ck = (float)a.hk, cv = (float)a.hk;
@@ -260,7 +375,7 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     __syncthreads();
     if (j + 1 < my) stage_load<AXIS, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
     cp_commit();
-    d2_line<N, float, float2>(vr, vi, t, scr + li * T::LSTRIDE, twN, dk2, ge);
+    d2_line_tab<N, false>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
     cp_wait_keep<1>();  // the momenta of this tile
     __syncthreads();
     float kes = 0.f;
