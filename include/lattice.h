@@ -306,11 +306,18 @@ int lat_ens_mark(lat_ens_t* e, int32_t slot);
 int lat_ens_mark_elapsed(lat_ens_t* e, int32_t slot_a, int32_t slot_b, double* ms);
 int lat_ens_launch_count(const lat_ens_t* e, int64_t* count);
 /* Times the persistent passes' block size and blocks per SM on this ensemble
- * (state saved and restored), keeps the fastest and caches it in cache_path
- * (JSON lines keyed by precision, SM count and the run sizes); NULL: no cache. */
+ * and, where every size class admits them, the streamed separable passes
+ * against the per-class cuFFT path (state saved and restored); keeps the
+ * fastest and caches it in cache_path (JSON lines keyed by precision, SM count
+ * and the run sizes); NULL: no cache. */
 int lat_ens_autotune(lat_ens_t* e, const char* cache_path);
 /* out[0] threads per block, out[1] blocks per SM of the persistent passes */
 int lat_ens_tuning_get(const lat_ens_t* e, int32_t out[2]);
+/* 1 when the ensemble's kicks run on the streamed separable passes: FP32,
+ * every size class 64, 96, 128, 192 or 256 with an even number of runs, two
+ * runs of a class forming one complex line (the default when admitted;
+ * LAT_ENS_CUFFT=1 in the environment at creation keeps cuFFT), else 0. */
+int lat_ens_sep_streamed(const lat_ens_t* e, int32_t* on);
 
 /* ------------------------------------------------- learned subgrid closure */
 /* No reference counterpart.  A coarse lattice evolved with a kick corrected

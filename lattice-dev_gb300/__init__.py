@@ -114,6 +114,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_ens_sync": ([P], I), "lat_ens_prepare": ([P, I, D, I], I), "lat_ens_mark": ([P, I], I),
         "lat_ens_mark_elapsed": ([P, I, I, dp], I), "lat_ens_launch_count": ([P, C.POINTER(I64)], I),
         "lat_ens_autotune": ([P, C.c_char_p], I), "lat_ens_tuning_get": ([P, C.POINTER(I)], I),
+        "lat_ens_sep_streamed": ([P, C.POINTER(I)], I),
         "lat_timing_enable": ([P, I], I), "lat_timing_read": ([P, I, dp, C.POINTER(I64)], I),
         "lat_timing_reset": ([P], I), "lat_mark": ([P, I], I), "lat_mark_elapsed": ([P, I, I, dp], I), "lat_launch_count": ([P, C.POINTER(I64)], I),
         "lat_device_ptr": ([P, I, C.POINTER(P)], I), "lat_host_alloc": ([C.POINTER(P), C.c_size_t], I),
@@ -592,6 +593,11 @@ class Ensemble:
         out = (C.c_int32 * 2)()
         _check(_lib.lat_ens_tuning_get(self._h, out))
         return list(out)
+
+    def sep_streamed(self) -> bool:
+        on = C.c_int32()
+        _check(_lib.lat_ens_sep_streamed(self._h, C.byref(on)))
+        return bool(on.value)
 
     def energies(self):
         out = np.zeros((len(self.sizes), NENERGY))

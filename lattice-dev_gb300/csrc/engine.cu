@@ -432,6 +432,8 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
   a.rb = red(h);
   a.nsm = h->nsm;
   a.stream = h->sep_stream ? 1 : 0;
+  a.runs = 0;                // the two fields of this lattice form one pair
+  a.pair_lines = a.nlines;
   int st;
   switch (n) {
     case 16: st = launch_sep_16(a, h->prec, axis, h->stream); break;

@@ -85,6 +85,13 @@ struct SepArgs {
   int64_t nlines;   // complex lines of this pass
   int nsm;          // SMs of the device (grid of the streamed passes)
   int stream;       // 1: the streamed passes of k_sep_stream.cuh (other buffer roles)
+  // streamed passes over pairs of independent one-field runs (ensembles):
+  // run 2i is line A and run 2i+1 line B, A and B nx*ny*nz apart, pairs
+  // 2*nx*ny*nz apart; nlines = pairs * pair_lines.  Minkowski only.
+  int runs;                 // 1: pairs of runs, 0: the two fields of one lattice (pair_lines = nlines)
+  int64_t pair_lines;       // lines of one pair along this pass
+  float* shift_a;           // [2 * pairs] shift of zs per run: written by pass X, read by pass Z
+  float* shift_b;           // [2 * pairs] phi at site 0 of each run: written by pass Z, read by pass X
   DevScalars* sc;
   RedBuf rb;
 };
@@ -96,6 +103,39 @@ int launch_sep_256(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_512(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int sep_stream_lines_128(int axis);  // lines per tile of the streamed passes (k_sep_stream.cuh)
 int sep_stream_lines_256(int axis);
+// streamed passes over pairs of one-field runs (ensembles), lines of n = 64,
+// 96, 128, 192 or 256 points (k_sep_<n>.cu)
+int launch_sep_runs_64(const SepArgs& a, int axis, cudaStream_t s);
+int launch_sep_runs_96(const SepArgs& a, int axis, cudaStream_t s);
+int launch_sep_runs_128(const SepArgs& a, int axis, cudaStream_t s);
+int launch_sep_runs_192(const SepArgs& a, int axis, cudaStream_t s);
+int launch_sep_runs_256(const SepArgs& a, int axis, cudaStream_t s);
+int sep_runs_lines_64(int axis);
+int sep_runs_lines_96(int axis);
+int sep_runs_lines_128(int axis);
+int sep_runs_lines_192(int axis);
+int sep_runs_lines_256(int axis);
+// lines per tile of the pass along `axis` for lines of n points; 0: n not supported
+inline int sep_runs_lines(int n, int axis) {
+  switch (n) {
+    case 64: return sep_runs_lines_64(axis);
+    case 96: return sep_runs_lines_96(axis);
+    case 128: return sep_runs_lines_128(axis);
+    case 192: return sep_runs_lines_192(axis);
+    case 256: return sep_runs_lines_256(axis);
+    default: return 0;
+  }
+}
+inline int launch_sep_runs(const SepArgs& a, int n, int axis, cudaStream_t s) {
+  switch (n) {
+    case 64: return launch_sep_runs_64(a, axis, s);
+    case 96: return launch_sep_runs_96(a, axis, s);
+    case 128: return launch_sep_runs_128(a, axis, s);
+    case 192: return launch_sep_runs_192(a, axis, s);
+    case 256: return launch_sep_runs_256(a, axis, s);
+    default: return set_error(LAT_ERR_UNSUPPORTED, "streamed separable passes: line length");
+  }
+}
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s);
 int sep_columns_16(int precision, int nf);
 int sep_columns_32(int precision, int nf);

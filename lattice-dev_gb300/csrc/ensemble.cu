@@ -132,6 +132,13 @@ __global__ void __launch_bounds__(256) ens_kmul_kernel(EnsArgs a) {
   }
 }
 
+// phi at site 0 of every run of a class: the first pass X's shifts
+__global__ void run_shift_init_kernel(const float* __restrict__ phi, int64_t nsite, int runs,
+                                      float* __restrict__ shift_b) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < runs) shift_b[r] = phi[(int64_t)r * nsite];
+}
+
 struct EnsGraph {
   int order;
   double dto;
@@ -157,6 +164,8 @@ struct lat_ens_s {
     cufftHandle r2c = 0, c2r = 0, r2c1 = 0, z2d1 = 0;
     bool have = false;
     double dx = 0, dk = 0;
+    float2* tw = nullptr;     // W_n^j (streamed separable passes)
+    float* shift = nullptr;   // [2][count] zs shift per run: written by pass X / pass Z
   };
   std::vector<Cls> cls;
   std::vector<int> run_cls;
@@ -171,6 +180,8 @@ struct lat_ens_s {
   double* spec_out = nullptr;
   unsigned int* spec_counter = nullptr;
   int grid = 0, block = 256;
+  bool sep_ok = false;  // every class can run the streamed separable passes (pairs of runs)
+  bool sep = false;     // and they are in use (else cuFFT per class)
   int64_t launches = 0;
   std::vector<EnsGraph> graphs;
   cudaEvent_t marks[16] = {};
@@ -294,17 +305,94 @@ int ens_fft(lat_ens_s* e, bool forward) {
   return LAT_OK;
 }
 
-int ens_exec(lat_ens_s* e, const std::vector<Op>& ops, double dto) {
-  auto pw = [&](int mode, double hk, double hd) {
-    EnsArgs a = base_args(e);
-    a.mode = mode;
-    for (int i = 0; i < a.nseg; ++i) {
-      const double dt = dto * e->cls[i].dx;  // dt = (dt/dx) dx per size class
-      a.seg[i].ck = hk * dt;
-      a.seg[i].cd = hd * dt;
+// One streamed separable pass (k_sep_stream.cuh) over every pair of runs of
+// class c: in place, kick weight hk and preceding drift hd in units of dt.
+int ens_sep_pass(lat_ens_s* e, const lat_ens_s::Cls& c, int axis, double hk, double hd, double dto) {
+  const int64_t n = c.n, n3 = n * n * n;
+  const double dt = dto * c.dx;
+  SepArgs a{};
+  a.nx = a.ny = a.nz = c.n;
+  a.nf = 1;
+  float* f = (float*)e->phi + c.site_off;
+  float* fc = (float*)e->phic + c.site_off;
+  float* p = (float*)e->pi + c.site_off;
+  float* z = (float*)e->lap + c.site_off;
+  a.phi = a.phi_out = f;
+  a.phic = a.phic_out = fc;
+  a.pi = a.pi_out = p;
+  a.lap = a.lap_out = z;
+  a.twN = c.tw;
+  a.dk2 = c.dk * c.dk;
+  a.model.model = e->base.model;
+  for (int i = 0; i < 4; ++i) a.model.p[i] = e->base.model_params[i];
+  a.hk = hk * dt;
+  a.hd = hd * dt;
+  a.Nd = (double)n3;
+  a.conf = 0;
+  a.pair_lines = n * n;
+  a.nlines = (int64_t)(c.count / 2) * a.pair_lines;
+  a.nsm = e->nsm;
+  a.stream = 1;
+  a.runs = 1;
+  a.shift_a = c.shift;
+  a.shift_b = c.shift + c.count;
+  a.sc = e->sc;
+  a.rb = e->rb;
+  return launch_sep_runs(a, c.n, axis, e->stream);
+}
+
+int ens_pw_args(lat_ens_s* e, int mode, double hk, double hd, double dto);
+
+// The op list on the streamed passes: every kick is the passes X (carrying
+// the preceding drift), Y and Z, per size class; the last drift is the
+// pointwise pass.  Minkowski lists only ((D) (K D+)*).
+int ens_exec_sep(lat_ens_s* e, const std::vector<Op>& ops, double dto) {
+  struct Grp { double hk, hd; };
+  std::vector<Grp> grp;
+  double lead = 0;
+  size_t i = 0;
+  while (i < ops.size() && ops[i].t == 'D') lead += ops[i++].h;
+  while (i < ops.size()) {
+    if (ops[i].t != 'K') return set_error(LAT_ERR_STATE, "ensemble op list: kick expected");
+    Grp g{ops[i++].h, 0.0};
+    while (i < ops.size() && ops[i].t == 'D') g.hd += ops[i++].h;
+    grp.push_back(g);
+  }
+  if (!grp.empty())
+    for (auto& c : e->cls) {
+      run_shift_init_kernel<<<(c.count + 127) / 128, 128, 0, e->stream>>>((const float*)e->phi + c.site_off,
+                                                                          (int64_t)c.n * c.n * c.n, c.count,
+                                                                          c.shift + c.count);
+      ++e->launches;
+      ECK(cudaGetLastError());
     }
-    return launch_ens_pw(e, a);
-  };
+  double pending = lead;
+  for (const Grp& g : grp) {
+    for (auto& c : e->cls) {
+      ERET(ens_sep_pass(e, c, 0, g.hk, pending, dto));
+      ERET(ens_sep_pass(e, c, 1, g.hk, 0.0, dto));
+      ERET(ens_sep_pass(e, c, 2, g.hk, 0.0, dto));
+    }
+    pending = g.hd;
+  }
+  if (pending != 0.0) ERET(ens_pw_args(e, 1, 0.0, pending, dto));
+  return LAT_OK;
+}
+
+int ens_pw_args(lat_ens_s* e, int mode, double hk, double hd, double dto) {
+  EnsArgs a = base_args(e);
+  a.mode = mode;
+  for (int i = 0; i < a.nseg; ++i) {
+    const double dt = dto * e->cls[i].dx;  // dt = (dt/dx) dx per size class
+    a.seg[i].ck = hk * dt;
+    a.seg[i].cd = hd * dt;
+  }
+  return launch_ens_pw(e, a);
+}
+
+int ens_exec(lat_ens_s* e, const std::vector<Op>& ops, double dto) {
+  if (e->sep) return ens_exec_sep(e, ops, dto);
+  auto pw = [&](int mode, double hk, double hd) { return ens_pw_args(e, mode, hk, hd, dto); };
   size_t i = 0;
   while (i < ops.size()) {
     if (ops[i].t == 'K' && i + 1 < ops.size() && ops[i + 1].t == 'D') {
@@ -358,10 +446,13 @@ int lat_ens_destroy(lat_ens_t* e) {
   for (auto& m : e->marks)
     if (m) cudaEventDestroy(m);
   for (auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
-  for (auto& c : e->cls)
+  for (auto& c : e->cls) {
     if (c.have) {
       cufftDestroy(c.r2c); cufftDestroy(c.c2r); cufftDestroy(c.r2c1); cufftDestroy(c.z2d1);
     }
+    if (c.tw) cudaFree(c.tw);
+    if (c.shift) cudaFree(c.shift);
+  }
   void* bufs[] = {e->phi, e->phic, e->pi, e->lap, e->Fk, e->work, e->sc, e->rb.partials, e->rb.counter,
                   e->spec_part, e->spec_out, e->spec_counter};
   for (void* b : bufs)
@@ -456,6 +547,33 @@ int lat_ens_create(lat_ens_t** out, const lat_config* base, int32_t nruns, const
     if ((st = plan(e, &c.z2d1, c.n, 1, CUFFT_Z2D))) return bail(st);
     c.have = true;
   }
+  // the streamed separable passes: FP32, every class of a supported side with
+  // an even run count, every pass in whole tiles (LAT_ENS_CUFFT=1: cuFFT)
+  const char* force_fft = getenv("LAT_ENS_CUFFT");
+  e->sep_ok = e->prec == LAT_FP32_KAHAN && !(force_fft && force_fft[0] == '1');
+  for (auto& c : e->cls) {
+    const int64_t n = c.n;
+    const int lx = sep_runs_lines(c.n, 0), ly = sep_runs_lines(c.n, 1), lz = sep_runs_lines(c.n, 2);
+    if (!lx || !ly || !lz || c.count % 2 || (n * n) % lx || (n * n) % ly || (n * n) % lz || n % ly || n % lz)
+      e->sep_ok = false;
+  }
+  if (e->sep_ok) {
+    for (auto& c : e->cls) {
+      if ((st = alloc((void**)&c.tw, (size_t)c.n * sizeof(float2)))) return bail(st);
+      if ((st = alloc((void**)&c.shift, (size_t)2 * c.count * sizeof(float)))) return bail(st);
+      std::vector<float> w(2 * c.n);
+      for (int j = 0; j < c.n; ++j) {
+        const long double ang = -6.283185307179586476925286766559L * (long double)j / (long double)c.n;
+        w[2 * j] = (float)cosl(ang);
+        w[2 * j + 1] = (float)sinl(ang);
+      }
+      if ((er = cudaMemcpyAsync(c.tw, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, e->stream)) !=
+          cudaSuccess)
+        return bail(cuda_fail(er, "ensemble twiddles"));
+      if ((er = cudaStreamSynchronize(e->stream)) != cudaSuccess) return bail(cuda_fail(er, "ensemble twiddles"));
+    }
+    e->sep = true;
+  }
   if ((er = cudaStreamSynchronize(e->stream)) != cudaSuccess) return bail(cuda_fail(er, "ensemble create"));
   *out = e;
   return LAT_OK;
@@ -546,6 +664,12 @@ int lat_ens_launch_count(const lat_ens_t* e, int64_t* count) {
   return LAT_OK;
 }
 
+int lat_ens_sep_streamed(const lat_ens_t* e, int32_t* on) {
+  if (!e || !on) return set_error(LAT_ERR_ARG, "null argument");
+  *on = e->sep ? 1 : 0;
+  return LAT_OK;
+}
+
 int lat_ens_tuning_get(const lat_ens_t* e, int32_t out[2]) {
   if (!e || !out) return set_error(LAT_ERR_ARG, "null argument");
   out[0] = e->block;
@@ -563,17 +687,18 @@ int lat_ens_autotune(lat_ens_t* e, const char* cache_path) {
     if (fp) {
       char line[4096];
       const std::string pat = "\"key\": \"" + key + "\"";
-      int blk = 0, bps = 0;
+      int blk = 0, bps = 0, sep = 0;
       bool found = false;
       while (fgets(line, sizeof(line), fp)) {
         if (!strstr(line, pat.c_str())) continue;
         const char* q = strstr(line, "\"block\":");
-        if (q && sscanf(q, "\"block\": %d, \"bps\": %d", &blk, &bps) == 2) found = true;
+        if (q && sscanf(q, "\"block\": %d, \"bps\": %d, \"sep\": %d", &blk, &bps, &sep) == 3) found = true;
       }
       fclose(fp);
       if (found && blk > 0 && bps > 0) {
         e->block = blk;
         e->grid = e->nsm * bps;
+        e->sep = e->sep_ok && sep != 0;
         for (auto& ge : e->graphs) cudaGraphExecDestroy(ge.exec);
         e->graphs.clear();
         return LAT_OK;
@@ -596,8 +721,18 @@ int lat_ens_autotune(lat_ens_t* e, const char* cache_path) {
   cudaEvent_t a = nullptr, b = nullptr;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  float best = 1e30f;
+  float best = 1e30f, tsep = 1e30f;
   int bblk = e->block, bgrid = e->grid;
+  if (e->sep_ok && st == LAT_OK) {  // the streamed separable passes
+    e->sep = true;
+    st = ens_exec(e, ops, 1e-4);  // warm-up
+    cudaEventRecord(a, e->stream);
+    for (int r = 0; r < 3 && st == LAT_OK; ++r) st = ens_exec(e, ops, 1e-4);
+    cudaEventRecord(b, e->stream);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&tsep, a, b);
+  }
+  e->sep = false;  // the cuFFT path with its pointwise shapes
   for (int blk : {128, 256})  // the persistent passes are built for at most 256 threads
     for (int bps : {1, 2, 4, 8}) {
       if (st != LAT_OK) break;
@@ -616,6 +751,7 @@ int lat_ens_autotune(lat_ens_t* e, const char* cache_path) {
   cudaEventDestroy(b);
   e->block = bblk;
   e->grid = bgrid;
+  e->sep = e->sep_ok && tsep < best;
   for (int i = 0; i < 3; ++i)
     if (saved[i]) cudaMemcpyAsync(live[i], saved[i], fb, cudaMemcpyDeviceToDevice, e->stream);
   cudaStreamSynchronize(e->stream);
@@ -627,7 +763,8 @@ int lat_ens_autotune(lat_ens_t* e, const char* cache_path) {
   if (cache_path) {
     FILE* fp = fopen(cache_path, "a");
     if (fp) {
-      fprintf(fp, "{\"key\": \"%s\", \"block\": %d, \"bps\": %d}\n", key.c_str(), e->block, e->grid / e->nsm);
+      fprintf(fp, "{\"key\": \"%s\", \"block\": %d, \"bps\": %d, \"sep\": %d}\n", key.c_str(), e->block,
+              e->grid / e->nsm, e->sep ? 1 : 0);
       fclose(fp);
     }
   }

@@ -44,15 +44,19 @@ template <> struct Split<64> { static constexpr int P = 8, Q = 8; };
 template <> struct Split<128> { static constexpr int P = 8, Q = 16; };
 template <> struct Split<256> { static constexpr int P = 16, Q = 16; };
 template <> struct Split<512> { static constexpr int P = 16, Q = 32; };
+template <> struct Split<96> { static constexpr int P = 4, Q = 24; };   // Q = 3 x 8 (dft24)
+template <> struct Split<192> { static constexpr int P = 8, Q = 24; };
 
 template <typename R> struct Cx;
 template <> struct Cx<float> {
   using T = float2;
   static __device__ __forceinline__ float2 tw(int j) { return make_float2(c_tw64f[j][0], c_tw64f[j][1]); }
+  static __device__ __forceinline__ float2 tw24(int j) { return make_float2(c_tw24f[j][0], c_tw24f[j][1]); }
 };
 template <> struct Cx<double> {
   using T = double2;
   static __device__ __forceinline__ double2 tw(int j) { return make_double2(c_tw64[j][0], c_tw64[j][1]); }
+  static __device__ __forceinline__ double2 tw24(int j) { return make_double2(c_tw24[j][0], c_tw24[j][1]); }
 };
 
 template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
@@ -133,13 +137,75 @@ __device__ __forceinline__ void dft_stage(Rt (&re)[R], Rt (&im)[R]) {
   if constexpr (LEN < R) dft_stage<R, INV, Rt, 2 * LEN>(re, im);
 }
 
-// In-register radix-2 DFT of R <= 64 points (R a power of two) on separate
-// real and imaginary arrays; W_len^k comes from the constant table.
+template <int R, bool INV, typename Rt>
+__device__ __forceinline__ void dft24(Rt (&re)[R], Rt (&im)[R]);
+
+// In-register DFT on separate real and imaginary arrays, natural order in and
+// out: radix 2 for R <= 64 points (R a power of two; W_len^k from the
+// constant table), and R = 24 = 3 x 8.
 template <int R, bool INV, typename Rt>
 __device__ __forceinline__ void dft(Rt (&re)[R], Rt (&im)[R]) {
-  static_assert(R >= 2 && R <= 64 && (R & (R - 1)) == 0, "register DFT length must be a power of two <= 64");
-  bitrev_perm<R>(re, im, std::make_integer_sequence<int, R>{});
-  dft_stage<R, INV, Rt, 2>(re, im);
+  if constexpr (R == 24) {
+    dft24<R, INV, Rt>(re, im);
+  } else {
+    static_assert(R >= 2 && R <= 64 && (R & (R - 1)) == 0, "register DFT length must be a power of two <= 64 or 24");
+    bitrev_perm<R>(re, im, std::make_integer_sequence<int, R>{});
+    dft_stage<R, INV, Rt, 2>(re, im);
+  }
+}
+
+// 24-point DFT by decimation in time over 3: the three 8-point DFTs of the
+// subsequences x[3 n1 + n2] (Y_n2[k1]), twiddles W_24^{n2 k1}, then 3-point
+// DFTs over n2 give X[k1 + 8 k2].  The 3-point DFT with w = exp(-+2 pi i / 3):
+// X0 = a + s, X1,2 = a - s/2 -+ i (sqrt(3)/2) d, s = b + c, d = b - c.
+template <int R, bool INV, typename Rt>
+__device__ __forceinline__ void dft24(Rt (&re)[R], Rt (&im)[R]) {
+  static_assert(R == 24, "dft24 takes 24 points");
+  Rt ar[3][8], ai[3][8];
+#pragma unroll
+  for (int n2 = 0; n2 < 3; ++n2) {
+#pragma unroll
+    for (int n1 = 0; n1 < 8; ++n1) {
+      ar[n2][n1] = re[3 * n1 + n2];
+      ai[n2][n1] = im[3 * n1 + n2];
+    }
+    dft<8, INV, Rt>(ar[n2], ai[n2]);
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < 3; ++n2) {
+#pragma unroll
+    for (int k1 = 1; k1 < 8; ++k1) {
+      const auto w = Cx<Rt>::tw24(n2 * k1);
+      const Rt xr = ar[n2][k1], xi = ai[n2][k1];
+      if (INV) {  // times conj(w)
+        ar[n2][k1] = xr * w.x + xi * w.y;
+        ai[n2][k1] = xi * w.x - xr * w.y;
+      } else {
+        ar[n2][k1] = xr * w.x - xi * w.y;
+        ai[n2][k1] = xr * w.y + xi * w.x;
+      }
+    }
+  }
+  const Rt h3 = (Rt)0.8660254037844386;  // sqrt(3)/2
+#pragma unroll
+  for (int k1 = 0; k1 < 8; ++k1) {
+    const Rt sr = ar[1][k1] + ar[2][k1], si = ai[1][k1] + ai[2][k1];
+    const Rt dr = (ar[1][k1] - ar[2][k1]) * h3, di = (ai[1][k1] - ai[2][k1]) * h3;
+    const Rt tr = ar[0][k1] - (Rt)0.5 * sr, ti = ai[0][k1] - (Rt)0.5 * si;
+    re[k1] = ar[0][k1] + sr;
+    im[k1] = ai[0][k1] + si;
+    if (INV) {  // X1 = t + i m, X2 = t - i m
+      re[k1 + 8] = tr - di;
+      im[k1 + 8] = ti + dr;
+      re[k1 + 16] = tr + di;
+      im[k1 + 16] = ti - dr;
+    } else {    // X1 = t - i m, X2 = t + i m
+      re[k1 + 8] = tr + di;
+      im[k1 + 8] = ti - dr;
+      re[k1 + 16] = tr - di;
+      im[k1 + 16] = ti + dr;
+    }
+  }
 }
 
 // Spectral second derivative of the complex line held as (re, im)[q] =

@@ -1,9 +1,10 @@
-// k_sep_stream.cuh -- streamed separable spectral passes for two FP32 fields.
+// k_sep_stream.cuh -- streamed separable spectral passes for pairs of FP32 lines.
 //
 // The spectral Laplacian of laplacian_3d (Pseudospec/openmp_dev/fftw_mod.f90:
 // 177-207) is the sum of one-dimensional second derivatives along x, y and z
-// (k_sep.cuh).  For two FP32 fields on lines of 128 or 256 points the engine
-// runs the three passes of a drift + kick in this form:
+// (k_sep.cuh).  For two FP32 fields (or, in ensembles, two independent
+// one-field runs of one size) the engine runs the three passes of a drift +
+// kick in this form, line A and line B forming one complex line:
 //
 //   pass X: drift of phi (Kahan), z = (phi - shift) - c written as the FP32
 //           array zs, pi += ck d2x(z)                       [PE, GEx, means]
@@ -13,17 +14,21 @@
 // with ck = hk a1^2, cv = hk a1^4, a1 = a - hg ysclp / 6 after the drift's
 // ysclp += hd sum(pi^2)/N / a^3 (hamiltonian_conformal.f90:86-174).  The
 // momenta accumulate the kick pass by pass, so no Laplacian array is kept:
-// per field and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
+// per line and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
 // needs ck before it has seen all momenta, so sum pi^2 comes from the pass Z
 // of the previous kick (or one reduction before the first pass X of a call).
+// Two fields use the lattice means as shifts; pairs of runs (Minkowski) use
+// each run's phi at site 0 as it was after the previous kick.
 //
 // Blocks are persistent.  A block reads the inputs of its tile from shared
 // memory into registers, refills the slot with the next tile's inputs by
 // cp.async at once, and runs the line transforms in a separate scratch, so the
-// next tile's HBM reads are in flight during the transforms.  X: 128-thread
-// blocks, 3 per SM, in which every warp stages and transforms its own lines
-// with warp barriers only; Y, Z: 256-thread blocks, 2 per SM, with a second
-// slot for the momenta, which are needed only after the transform.
+// next tile's HBM reads are in flight during the transforms.  Pass X: 128
+// threads per block; every warp stages and transforms its own lines with warp
+// barriers only.  Passes Y, Z: 16 (256-point lines) or 32 x-columns per
+// block, with a second slot for the momenta, which are needed only after the
+// transform.  Every update of a tile is written by the block that read it,
+// so the passes also run in place.
 #pragma once
 #include "k_sep.cuh"
 
@@ -44,6 +49,7 @@ template <int N, bool WARP, typename Acc>
 __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im)[Split<N>::Q], int t, float2* sl,
                                             const float2* tf, const float2* ti, const float* fk, Acc& ge) {
   constexpr int P = Split<N>::P, Q = Split<N>::Q, G = Q / P, S = P + 1;
+  static_assert(Q % P == 0, "the transform needs Q a multiple of P");
   auto sync = [] {
     if (WARP) __syncwarp();
     else __syncthreads();
@@ -110,8 +116,8 @@ __device__ __forceinline__ void build_tables(const float2* twN, float dk2, float
                                              int nthreads) {
   constexpr int P = Split<N>::P, Q = Split<N>::Q;
   for (int j = tid; j < P * Q; j += nthreads) {
-    tf[j] = twN[((j % P) * (j / P)) & (N - 1)];
-    if (P != Q) ti[j] = twN[((j / Q) * (j % Q)) & (N - 1)];
+    tf[j] = twN[((j % P) * (j / P)) % N];
+    if (P != Q) ti[j] = twN[((j / Q) * (j % Q)) % N];
   }
   for (int k = tid; k < N; k += nthreads) {
     const int f = k <= N / 2 ? k : k - N;
@@ -122,93 +128,100 @@ __device__ __forceinline__ void build_tables(const float2* twN, float dk2, float
 template <int AXIS, int N>
 struct STile {
   static constexpr int P = Split<N>::P, Q = Split<N>::Q;
-  static constexpr int THREADS = AXIS == 0 ? 128 : 256, LINES = THREADS / P;
-  static constexpr int MINB = AXIS == 0 ? 3 : 2;  // blocks per SM
+  static constexpr int LINES_YZ = N == 256 ? 16 : 32;  // x-columns of a Y, Z tile (64 or 128 bytes)
+  static constexpr int THREADS = AXIS == 0 ? 128 : P * LINES_YZ, LINES = THREADS / P;
   // X: one staged row per line (padded by P floats so the 32/P lines of a
   // warp start in different banks); Y, Z: one row of LINES x-columns per
   // position along the line
   static constexpr int RS = AXIS == 0 ? N + P : LINES;
   static constexpr int ROWS = AXIS == 0 ? LINES : N;
   static constexpr int ARR = ROWS * RS;               // floats per staged array
-  static constexpr int N_EARLY = AXIS == 0 ? 6 : 2;   // X: phi, c, pi of both fields; Y, Z: zs
-  static constexpr int N_LATE = AXIS == 0 ? 0 : 2;    // Y, Z: pi of both fields
-  static constexpr int LSTRIDE = Tile<float, 2, AXIS, N>::LSTRIDE;
+  static constexpr int N_EARLY = AXIS == 0 ? 6 : 2;   // X: phi, c, pi of both lines; Y, Z: zs
+  static constexpr int N_LATE = AXIS == 0 ? 0 : 2;    // Y, Z: pi of both lines
+  // transpose scratch per line, in complex: Q rows of P + 1, padded so the
+  // lines a warp touches at once start in different banks
+  static constexpr int LANES = AXIS == 0 ? P : (32 / LINES > 0 ? 32 / LINES : 1);
+  static constexpr int LINE_WORDS = LANES * 2 >= 32 ? 0 : LANES * 2;
+  static constexpr int lstride_for(int pad) {
+    return ((Q * (P + 1) + pad) * 2) % 32 == LINE_WORDS ? Q * (P + 1) + pad : lstride_for(pad + 1);
+  }
+  static constexpr int LSTRIDE = lstride_for(0);
   static constexpr int E_OFF = 0, L_OFF = N_EARLY * ARR, S_OFF = L_OFF + N_LATE * ARR;  // floats
   static constexpr int TF_OFF = S_OFF + LINES * LSTRIDE * 2;  // twiddle tables W_N^{t kq}, W_N^{mp kq}
   static constexpr int TI_OFF = P == Q ? TF_OFF : TF_OFF + 2 * N;
   static constexpr int FK_OFF = TI_OFF + 2 * N;                   // (f dk)^2
   static constexpr int SMEM = (FK_OFF + N) * 4;
-  // MINB blocks, each with its dynamic and static (reduction) shared memory
-  // and the 1 KB the SM reserves per block, fit in 228 KB
-  static_assert(MINB * (SMEM + 1300 + 1024) <= 228 * 1024, "blocks per SM must fit in shared memory");
+  // blocks per SM: dynamic and static (reduction) shared memory plus the
+  // 1 KB the SM reserves per block, within 228 KB; at most 3
+  static constexpr int PER_BLOCK = SMEM + 1300 + 1024;
+  static constexpr int MINB = (228 * 1024) / PER_BLOCK > 3 ? 3 : (228 * 1024) / PER_BLOCK;
+  static_assert(MINB >= 1, "a block must fit in shared memory");
   static_assert(RS % 4 == 0 && N % 4 == 0, "staged rows must hold whole 16-byte copies");
 };
 
-// Copy the early (part 0) or late (part 1) inputs of tile `tile` into the
-// slot `dst` with 16-byte cp.async copies.  Thread tid always copies chunk
-// tid % CPR of rows tid / CPR + j * (THREADS / CPR), so its addresses are one
-// base per array plus compile-time steps.
+// First-line geometry of a tile: the pair it belongs to and the offset of
+// line A's first site.  Two fields: one pair (pair_lines = nlines).
+template <int AXIS>
+__device__ __forceinline__ int64_t tile_base(const SepArgs& a, int64_t l0, int64_t& pair) {
+  const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
+  pair = l0 / a.pair_lines;
+  const int64_t r = l0 % a.pair_lines;
+  const int64_t pbase = pair * 2 * Ns;
+  if constexpr (AXIS == 0) return pbase + r * a.nx;
+  const int64_t plane = (int64_t)a.nx * a.ny;
+  const int64_t x0 = r % a.nx, o = r / a.nx;
+  return pbase + (AXIS == 1 ? o * plane : o * a.nx) + x0;
+}
+
+// Passes Y, Z: copy the early (part 0: zs) or late (part 1: pi) inputs of
+// tile `tile`, both lines, into a slot with 16-byte cp.async copies.  Thread
+// tid copies chunk tid % CPR of rows tid / CPR + j * (THREADS / CPR).
 template <int AXIS, int N>
 __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t tile, int part, int tid) {
   using T = STile<AXIS, N>;
-  constexpr int CPR = (AXIS == 0 ? N : T::RS) / 4;  // 16-byte chunks per staged row
+  constexpr int CPR = T::RS / 4;  // 16-byte chunks per staged row
   constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
   static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
   const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
   const int row0 = tid / CPR, ch = tid % CPR;
-  const int64_t l0 = tile * T::LINES;
-  int64_t src0, stride;
-  if constexpr (AXIS == 0) {
-    src0 = (l0 + row0) * a.nx + ch * 4;  // rows = lines l0 .. l0 + LINES - 1
-    stride = a.nx;
-  } else {
-    const int64_t plane = (int64_t)a.nx * a.ny;
-    const int64_t x0 = l0 % a.nx, o = l0 / a.nx;
-    stride = AXIS == 1 ? a.nx : plane;
-    src0 = (AXIS == 1 ? o * plane : o * a.nx) + x0 + row0 * stride + ch * 4;
-  }
+  int64_t pair;
+  const int64_t base = tile_base<AXIS>(a, tile * T::LINES, pair);
+  const int64_t stride = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
   const int64_t jstep = RPJ * stride;
   float* d0 = dst + row0 * T::RS + ch * 4;
-  // arrays: X [field][phi, c, pi]; Y, Z early [field] zs, late [field] pi
-  constexpr int NA = AXIS == 0 ? 6 : 2;
-  constexpr int PERF = AXIS == 0 ? 3 : 1;
+  const float* src = static_cast<const float*>(part == 0 ? a.lap : a.pi) + base + row0 * stride + ch * 4;
 #pragma unroll
-  for (int arr = 0; arr < NA; ++arr) {
-    const int f = arr / PERF, k = arr % PERF;
-    const void* sp = AXIS == 0 ? (k == 0 ? a.phi : (k == 1 ? a.phic : a.pi)) : (part == 0 ? a.lap : a.pi);
-    const float* src = static_cast<const float*>(sp) + f * Ns + src0;
-    float* d = d0 + arr * T::ARR;
+  for (int f = 0; f < 2; ++f) {
 #pragma unroll
-    for (int j = 0; j < STEPS; ++j) cp16(d + j * RPJ * T::RS, src + j * jstep);
+    for (int j = 0; j < STEPS; ++j) cp16(d0 + f * T::ARR + j * RPJ * T::RS, src + f * Ns + j * jstep);
   }
 }
 
 // Pass X staging by one warp: the rows of its own 32/P lines of tile `tile`
-// (6 arrays: [field][phi, c, pi]), so the warp waits only for its own copies.
+// (6 arrays: [line A, B][phi, c, pi]), so the warp waits only for its copies.
 template <int N>
 __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64_t tile, int warp, int lane) {
   using T = STile<0, N>;
   constexpr int LPW = 32 / T::P, CPR = N / 4;  // lines per warp, 16-byte chunks per row
-  static_assert(CPR % 32 == 0 || 32 % CPR == 0, "a row is whole lanes");
   const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
-  const int64_t r0 = tile * T::LINES + warp * LPW;  // first line (row) of the warp
+  int64_t pair;
+  const int64_t r0 = tile_base<0>(a, tile * T::LINES + warp * LPW, pair);  // first site of the warp's rows
   float* d0 = dst + warp * LPW * T::RS;
 #pragma unroll
   for (int arr = 0; arr < 6; ++arr) {
     const int f = arr / 3, k = arr % 3;
     const void* sp = k == 0 ? a.phi : (k == 1 ? a.phic : a.pi);
-    const float* src = static_cast<const float*>(sp) + f * Ns + r0 * a.nx;
+    const float* src = static_cast<const float*>(sp) + f * Ns + r0;
 #pragma unroll
-    for (int r = 0; r < LPW; ++r) {
-#pragma unroll
-      for (int c = lane; c < CPR; c += 32)
-        cp16(d0 + arr * T::ARR + r * T::RS + c * 4, src + (int64_t)r * a.nx + c * 4);
+    for (int i = lane; i < LPW * CPR; i += 32) {
+      const int r = i / CPR, c = i % CPR;
+      cp16(d0 + arr * T::ARR + r * T::RS + c * 4, src + (int64_t)r * a.nx + c * 4);
     }
   }
 }
 
 // Pass X: drift, zs and the x part of the kick.
-template <int N>
+template <int N, bool RUNS>
 __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     sep_stream_x(const __grid_constant__ SepArgs a) {
   using T = STile<0, N>;
@@ -234,12 +247,15 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   float* __restrict__ zs_o = static_cast<float*>(a.lap_out);
   const DevScalars* sc = a.sc;
-  const double shAd = __ldcg(&sc->mean[0]), shBd = __ldcg(&sc->mean[1]);
-  const float shA = (float)shAd, shB = (float)shBd;
+  double shAd = 0.0, shBd = 0.0;
+  if (!RUNS) {
+    shAd = __ldcg(&sc->mean[0]);
+    shBd = __ldcg(&sc->mean[1]);
+  }
   const bool drift = a.hd != 0.0;
   double a0 = 1.0, ap0 = 0.0, ke = 0.0;
   float cd = (float)a.hd, ck = (float)a.hk;
-  if (a.conf) {
+  if (!RUNS && a.conf) {
     a0 = __ldcg(&sc->a);
     ke = __ldcg(&sc->ke_cur);
     ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
@@ -248,9 +264,34 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     ck = (float)(a.hk * a1 * a1);
   }
   KSum ge, pe, mA, mB;
+  // pairs of runs: each run's shift is its phi at site 0 after the previous
+  // kick (shift_b), loaded one tile ahead; the block holding a pair's first
+  // tile passes it on to pass Z (shift_a)
+  float nshA = 0.f, nshB = 0.f;
+  if (RUNS && my > 0) {
+    const int64_t p0 = (int64_t)blockIdx.x * LINES / a.pair_lines;
+    nshA = __ldcg(a.shift_b + 2 * p0);
+    nshB = __ldcg(a.shift_b + 2 * p0 + 1);
+  }
   for (int64_t j = 0; j < my; ++j) {
-    const int64_t l = ((int64_t)blockIdx.x + j * gridDim.x) * LINES + li;
-    const int64_t offA = l * a.nx, offB = Nsite + offA;
+    int64_t pair;
+    const int64_t l0 = ((int64_t)blockIdx.x + j * gridDim.x) * LINES;
+    const int64_t offA = tile_base<0>(a, l0 + li, pair);
+    const int64_t offB = Nsite + offA;
+    float shA = (float)shAd, shB = (float)shBd;
+    if (RUNS) {
+      shA = nshA;
+      shB = nshB;
+      if (tid == 0 && l0 % a.pair_lines == 0) {
+        a.shift_a[2 * pair] = shA;
+        a.shift_a[2 * pair + 1] = shB;
+      }
+      if (j + 1 < my) {
+        const int64_t pn = (l0 + (int64_t)gridDim.x * LINES) / a.pair_lines;
+        nshA = __ldcg(a.shift_b + 2 * pn);
+        nshB = __ldcg(a.shift_b + 2 * pn + 1);
+      }
+    }
     cp_wait_keep<0>();
     __syncwarp();
     float vr[Q], vi[Q], pA[Q], pB[Q];
@@ -271,20 +312,24 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       phi_o[offB + pos] = fB;
       phic_o[offA + pos] = cA;
       phic_o[offB + pos] = cB;
-      if (a.conf) {
-        float ff[2] = {fA, fB};
-        pes += model_v<float, 2>(a.model, ff);
+      if (!RUNS) {
+        if (a.conf) {
+          float ff[2] = {fA, fB};
+          pes += model_v<float, 2>(a.model, ff);
+        }
+        mAs += fA;
+        mBs += fB;
       }
-      mAs += fA;
-      mBs += fB;
       vr[q] = (fA - shA) - cA;
       vi[q] = (fB - shB) - cB;
       zs_o[offA + pos] = vr[q];
       zs_o[offB + pos] = vi[q];
     }
-    pe.add(pes);
-    mA.add(mAs);
-    mB.add(mBs);
+    if (!RUNS) {
+      pe.add(pes);
+      mA.add(mAs);
+      mB.add(mBs);
+    }
     __syncwarp();  // the warp's rows are free: stage its rows of the next tile
     if (j + 1 < my) stage_rows_x<N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, warp, lane);
     cp_commit();
@@ -297,6 +342,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     }
   }
   cp_wait_all();
+  if (RUNS) return;
   double vals[4] = {pe.val(), ge.val(), mA.val(), mB.val()}, tot[4];
   if (grid_reduce<4>(vals, a.rb, tot)) {
     DevScalars* w = a.sc;
@@ -316,7 +362,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
 
 // Passes Y (AXIS 1) and Z (AXIS 2): the y part of the kick; the z part with
 // the potential force, which completes the kick and its ysclp update.
-template <int AXIS, int N>
+template <int AXIS, int N, bool RUNS>
 __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     sep_stream_yz(const __grid_constant__ SepArgs a) {
   using T = STile<AXIS, N>;
@@ -339,14 +385,17 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
 
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
-  const int64_t plane = (int64_t)a.nx * a.ny;
-  const int64_t st = AXIS == 1 ? a.nx : plane;
+  const int64_t st = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   const DevScalars* sc = a.sc;
-  const float zshA = (float)__ldcg(&sc->zsh[0]), zshB = (float)__ldcg(&sc->zsh[1]);
+  float zshA = 0.f, zshB = 0.f;
+  if (!RUNS && AXIS == 2) {
+    zshA = (float)__ldcg(&sc->zsh[0]);
+    zshB = (float)__ldcg(&sc->zsh[1]);
+  }
   double a0 = 1.0, ap0 = 0.0, a1 = 1.0;
   float ck = (float)a.hk, cv = (float)a.hk;
-  if (a.conf) {
+  if (!RUNS && a.conf) {
     a0 = __ldcg(&sc->a);
     ap0 = __ldcg(&sc->ap);
     a1 = a0 - a.hg * ap0 / 6.0;  // Hamiltonian_grav_kinetic before the kick
@@ -354,10 +403,25 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     cv = (float)(a.hk * a1 * a1 * a1 * a1);
   }
   KSum ge, ke;
+  float nzA = 0.f, nzB = 0.f;  // pairs of runs, pass Z: the next tile's shifts, loaded one tile ahead
+  if (RUNS && AXIS == 2 && my > 0) {
+    const int64_t p0 = (int64_t)blockIdx.x * LINES / a.pair_lines;
+    nzA = __ldcg(a.shift_a + 2 * p0);
+    nzB = __ldcg(a.shift_a + 2 * p0 + 1);
+  }
   for (int64_t j = 0; j < my; ++j) {
-    const int64_t l = ((int64_t)blockIdx.x + j * gridDim.x) * LINES + li;
-    const int64_t x = l % a.nx, o = l / a.nx;
-    const int64_t offA = (AXIS == 1 ? o * plane : o * a.nx) + x, offB = Nsite + offA;
+    const int64_t l0 = ((int64_t)blockIdx.x + j * gridDim.x) * LINES;
+    int64_t pair;
+    const int64_t offA = tile_base<AXIS>(a, l0, pair) + li, offB = Nsite + offA;
+    if (RUNS && AXIS == 2) {
+      zshA = nzA;
+      zshB = nzB;
+      if (j + 1 < my) {
+        const int64_t pn = (l0 + (int64_t)gridDim.x * LINES) / a.pair_lines;
+        nzA = __ldcg(a.shift_a + 2 * pn);
+        nzB = __ldcg(a.shift_a + 2 * pn + 1);
+      }
+    }
     cp_wait_keep<1>();  // zs of this tile (its momenta may still be in flight)
     __syncthreads();
     float vr[Q], vi[Q];
@@ -370,6 +434,13 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
       if constexpr (AXIS == 2) {
         hA[q] = vr[q] + zshA;  // phi - c
         hB[q] = vi[q] + zshB;
+      }
+    }
+    if constexpr (RUNS && AXIS == 2) {
+      if (t == 0 && li == 0 && l0 % a.pair_lines == 0) {
+        // site 0 of both runs of the pair: the next pass X's shifts
+        a.shift_b[2 * pair] = hA[0];
+        a.shift_b[2 * pair + 1] = hB[0];
       }
     }
     __syncthreads();
@@ -388,22 +459,33 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
         pA = pA + ck * vr[q];
         pB = pB + ck * vi[q];
       } else {
-        float ff[2] = {hA[q], hB[q]}, dv[2];
-        model_dv<float, 2>(a.model, ff, dv);
-        pA = pA + (ck * vr[q] - cv * dv[0]);
-        pB = pB + (ck * vi[q] - cv * dv[1]);
-        kes += pA * pA + pB * pB;
+        float dA, dB;
+        if constexpr (RUNS) {  // two independent runs: each its own potential
+          float fa[1] = {hA[q]}, fb[1] = {hB[q]}, da[1], db[1];
+          model_dv<float, 1>(a.model, fa, da);
+          model_dv<float, 1>(a.model, fb, db);
+          dA = da[0];
+          dB = db[0];
+        } else {
+          float ff[2] = {hA[q], hB[q]}, dv[2];
+          model_dv<float, 2>(a.model, ff, dv);
+          dA = dv[0];
+          dB = dv[1];
+        }
+        pA = pA + (ck * vr[q] - cv * dA);
+        pB = pB + (ck * vi[q] - cv * dB);
+        if (!RUNS) kes += pA * pA + pB * pB;
       }
       pi_o[sA] = pA;
       pi_o[sB] = pB;
     }
-    if (AXIS == 2) ke.add(kes);
+    if (AXIS == 2 && !RUNS) ke.add(kes);
     __syncthreads();
     if (j + 1 < my) stage_load<AXIS, N>(a, ls, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 1, tid);
     cp_commit();
   }
   cp_wait_all();
-  if (!a.conf) return;
+  if (RUNS || !a.conf) return;
   if constexpr (AXIS == 1) {
     double vals[1] = {ge.val()}, tot[1];
     if (grid_reduce<1>(vals, a.rb, tot)) a.sc->gsum[1] = tot[0];
@@ -441,19 +523,21 @@ int stream_lines(int axis) {
   return axis == 0 ? STile<0, N>::LINES : (axis == 1 ? STile<1, N>::LINES : STile<2, N>::LINES);
 }
 
-template <int N>
+template <int N, bool RUNS>
 int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
   const int lines = stream_lines<N>(axis);
-  if (a.nf != 2 || a.nlines % lines || (axis != 0 && a.nx % lines))
+  if (a.pair_lines <= 0 || a.nlines <= 0 || a.nlines % a.pair_lines || a.pair_lines % lines ||
+      (axis != 0 && a.nx % lines) || (!RUNS && (a.nf != 2 || a.nlines != a.pair_lines)) ||
+      (RUNS && (a.conf || !a.shift_a || !a.shift_b)))
     return set_error(LAT_ERR_STATE, "streamed separable pass: lines do not form whole tiles");
   const int64_t ntiles = a.nlines / lines;
   switch (axis) {
-    case 0: return stream_launch(sep_stream_x<N>, STile<0, N>::SMEM, STile<0, N>::THREADS, STile<0, N>::MINB,
-                                 ntiles, a, s);
-    case 1: return stream_launch(sep_stream_yz<1, N>, STile<1, N>::SMEM, STile<1, N>::THREADS, STile<1, N>::MINB,
-                                 ntiles, a, s);
-    default: return stream_launch(sep_stream_yz<2, N>, STile<2, N>::SMEM, STile<2, N>::THREADS, STile<2, N>::MINB,
-                                  ntiles, a, s);
+    case 0: return stream_launch(sep_stream_x<N, RUNS>, STile<0, N>::SMEM, STile<0, N>::THREADS,
+                                 STile<0, N>::MINB, ntiles, a, s);
+    case 1: return stream_launch(sep_stream_yz<1, N, RUNS>, STile<1, N>::SMEM, STile<1, N>::THREADS,
+                                 STile<1, N>::MINB, ntiles, a, s);
+    default: return stream_launch(sep_stream_yz<2, N, RUNS>, STile<2, N>::SMEM, STile<2, N>::THREADS,
+                                  STile<2, N>::MINB, ntiles, a, s);
   }
 }
 

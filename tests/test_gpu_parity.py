@@ -490,22 +490,28 @@ def test_defrost_symp6_constant_and_symp8(engine, orc):
         g.symp(8, 0.025, 1)
 
 
-def test_fp32_kahan_tracks_fp64_oracle(engine, orc):
-    """The FP32-Kahan engine (both spectral paths) against the FP64 oracle."""
+@pytest.mark.parametrize("shape,steps", [((64, 32, 32), 20), ((128, 128, 128), 4)])
+def test_fp32_kahan_tracks_fp64_oracle(engine, orc, shape, steps):
+    """The FP32-Kahan engine (cuFFT path and separable passes: the
+    one-tile-per-block kind at 64x32x32, the streamed kind at 128^3) against
+    the FP64 oracle."""
+    nx, ny, nz = shape
     for impl in (L.SPEC_IMPL_CUFFT, L.SPEC_IMPL_SEPARABLE):
-        c = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
-                          precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0),
-                          spectral_impl=impl)
+        c = L.make_config(shape, nfld=2, length=16.0 * nx / 64, laplacian=L.LAP_SPECTRAL,
+                          background=L.BG_CONFORMAL, precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2,
+                          model_params=(1.0, 2.0), spectral_impl=impl)
         g = engine.Lattice(c)
-        c64 = L.make_config((64, 32, 32), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL,
+        if impl == L.SPEC_IMPL_SEPARABLE:
+            assert g.sep_streamed() == (nx == 128)
+        c64 = L.make_config(shape, nfld=2, length=16.0 * nx / 64, laplacian=L.LAP_SPECTRAL,
                             background=L.BG_CONFORMAL, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
         o = orc.Oracle(c64)
-        f, p = random_state((2, 32, 32, 64), seed=17, mean=1.0, amp=0.01)
+        f, p = random_state((2, nz, ny, nx), seed=17, mean=1.0, amp=0.01)
         for obj in (g, o):
             obj.set_state(f, p)
             obj.set_scale_factor(1.0, 0.0)
             obj.calc_metric()
-            obj.symp(4, 0.02, 20)
+            obj.symp(4, 0.02, steps)
         gf, gp = g.get_state()
         of, op = o.get_state()
         # fluctuations of ~1e-2 around 1: compare the fluctuation, not the mean;

@@ -209,3 +209,41 @@ def test_streamed_passes_match_classic(engine, shape, conf, monkeypatch):
         assert abs(aa - ab) <= 1e-9 * ab and abs(apa - apb) <= 1e-7 * abs(apb)
     ea, eb = a.energies(), b.energies()
     assert abs(ea[L.E_RHO] - eb[L.E_RHO]) <= 1e-6 * abs(eb[L.E_RHO])
+
+
+def test_ensemble_streamed_passes(engine, monkeypatch):
+    """Ensembles whose size classes admit the streamed separable passes (two
+    runs of a class as one complex line, 24-point register DFTs for 96 and 192)
+    against the FP64 ensemble (cuFFT) and the FP32 cuFFT ensemble from the
+    same initial states."""
+    sizes = [64, 96, 64, 96, 128, 192, 128, 192]
+    seeds = [7000 + r for r in range(len(sizes))]
+
+    def run(prec, cufft):
+        if cufft:
+            monkeypatch.setenv("LAT_ENS_CUFFT", "1")
+        base = L.make_config(16, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=prec, model=L.MODEL_PHI4)
+        ens = engine.Ensemble(base, sizes)
+        monkeypatch.delenv("LAT_ENS_CUFFT", raising=False)
+        assert ens.sep_streamed() == (prec == L.FP32_KAHAN and not cufft)
+        ens.init_vacuum(seeds, 1.0, 0.0, 3.0, amp=1e-4, kcut_frac=0.5)
+        ens.symp(4, 1.0 / 20, 6)
+        ens.symp(2, 1.0 / 20, 3)
+        out = [ens.state(r) for r in range(len(sizes))]
+        E = ens.energies()
+        ens.close()
+        return out, E
+
+    s64, E64 = run(L.FP64, True)
+    s32, E32 = run(L.FP32_KAHAN, False)
+    c32, _ = run(L.FP32_KAHAN, True)
+    for r in range(len(sizes)):
+        ref_f, ref_p = s64[r]
+        m = ref_f.mean()
+        err_s = rel_err(s32[r][0] - m, ref_f - m)
+        err_c = rel_err(c32[r][0] - m, ref_f - m)
+        # fluctuations of ~5e-3 around phi = 1, resolved by FP32 to ~1e-5
+        assert err_s <= 2e-4, (r, sizes[r], err_s)
+        assert err_s <= 2 * err_c + 1e-5, (r, sizes[r], err_s, err_c)
+        assert rel_err(s32[r][1], ref_p) <= 2e-4, r
+        assert abs(E32[r, L.E_RHO] - E64[r, L.E_RHO]) <= 1e-5 * abs(E64[r, L.E_RHO])
