@@ -137,6 +137,28 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], const RedBuf rb, do
   return true;
 }
 
+// Block sums of NV doubles written to out[blockIdx.x * NV + i] by thread 0:
+// the partials of a reduction that a later kernel completes in block order
+// (no fence or arrival counter in the pass).  All threads must call it.
+template <int NV>
+__device__ __forceinline__ void block_partials(const double (&v)[NV], double* out) {
+  __shared__ double sh[NV][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double x = warp_sum(v[i]);
+    if (lane == 0) sh[i][wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      const double x = warp_sum(lane < nw ? sh[i][lane] : 0.0);
+      if (lane == 0) out[(size_t)blockIdx.x * NV + i] = x;
+    }
+  }
+}
+
 __device__ __forceinline__ bool bad(double x) { return !(x - x == 0.0); }
 
 // ---------------------------------------------------------------- models

@@ -396,10 +396,11 @@ int exec_plain(lat_s* h, const std::vector<Op>& ops) {
 }
 
 // One separable spectral pass (k_sep.cuh) along `axis`.
-int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
+int sep_pass(lat_s* h, int axis, double hk, double hg, double hd, int* grid_out = nullptr) {
   static const int kcls[3] = {LAT_K_SEP_X, LAT_K_SEP_Y, LAT_K_SEP_Z};
   Timed t(h, kcls[axis]);
   SepArgs a{};
+  a.grid_out = grid_out;
   a.nx = h->nx; a.ny = h->ny; a.nz = h->nz; a.nf = h->nf;
   a.phi = h->fld[h->cur];
   a.phic = h->fldc;
@@ -407,7 +408,10 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
   a.phi_out = h->fld[1 - h->cur];
   a.phic_out = h->fldc_alt;
   a.pi_out = h->fldp_alt;
-  if (h->sep_stream) {  // lap holds zs, written by X; every pass updates the momenta
+  if (h->sep_stream) {  // in place (every tile is updated by the block that read it); lap holds zs
+    a.phi_out = h->fld[h->cur];
+    a.phic_out = h->fldc;
+    a.pi_out = h->fldp;
     a.lap = h->lap;
     a.lap_out = h->lap;
   } else {
@@ -444,12 +448,13 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd) {
     case 512: st = launch_sep_512(a, h->prec, axis, h->stream); break;
     default: return set_error(LAT_ERR_UNSUPPORTED, "separable pass length");
   }
-  if (st != LAT_OK) return st;
+  if (st != LAT_OK || h->sep_stream) return st;
   if (axis == 0) {  // drifted fields now live in the second buffers
     h->cur = 1 - h->cur;
     std::swap(h->fldc, h->fldc_alt);
+  } else if (axis == 2) {  // kicked momenta
+    std::swap(h->fldp, h->fldp_alt);
   }
-  if (axis == 2 || h->sep_stream) std::swap(h->fldp, h->fldp_alt);  // (partly) kicked momenta
   return LAT_OK;
 }
 
@@ -490,12 +495,30 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
     RET(launch_pi2_sum(h->fldp, (int64_t)h->nf * h->N, h->sc, red(h), 2 * h->nsm, h->stream));
   }
   for (const Grp& g : grp) {
-    // the streamed pass X starts the kick, so it takes the group's kick and
-    // grav-kinetic weights too
-    if (h->sep_stream) RET(sep_pass(h, 0, g.hk, g.hg, pending));
-    else RET(sep_pass(h, 0, 0.0, 0.0, pending));
-    RET(sep_pass(h, 1, h->sep_stream ? g.hk : 0.0, h->sep_stream ? g.hg : 0.0, 0.0));
-    RET(sep_pass(h, 2, g.hk, g.hg, 0.0));
+    if (h->sep_stream) {
+      // every streamed pass takes the kick's weights and pass X's drift (the
+      // scalar block keeps the pre-kick state until the finalize after Z)
+      SepFinArgs f{};
+      RET(sep_pass(h, 0, g.hk, g.hg, pending, &f.gx));
+      RET(sep_pass(h, 1, g.hk, g.hg, pending, &f.gy));
+      RET(sep_pass(h, 2, g.hk, g.hg, pending, &f.gz));
+      f.sc = h->sc;
+      f.part = red(h).partials;
+      f.hk = g.hk;
+      f.hg = g.hg;
+      f.hd = pending;
+      f.Nd = (double)h->N;
+      f.conf = conf ? 1 : 0;
+      if (!conf) f.gy = f.gz = 0;  // a static background writes no Y, Z partials
+      if (4 * f.gx > SEP_PART_Y || f.gy > SEP_PART_Z - SEP_PART_Y || (SEP_PART_Z + 2 * f.gz) > 16 * h->red_cap)
+        return set_error(LAT_ERR_STATE, "streamed separable passes: partial sums exceed the reduction buffer");
+      Timed t(h, LAT_K_OTHER);
+      RET(launch_sep_finalize(f, h->stream));
+    } else {
+      RET(sep_pass(h, 0, 0.0, 0.0, pending));
+      RET(sep_pass(h, 1, 0.0, 0.0, 0.0));
+      RET(sep_pass(h, 2, g.hk, g.hg, 0.0));
+    }
     pending = g.hd;
   }
   if (pending != 0.0) RET(exec_drift(h, pending));

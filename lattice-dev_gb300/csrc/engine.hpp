@@ -92,6 +92,7 @@ struct SepArgs {
   int64_t pair_lines;       // lines of one pair along this pass
   float* shift_a;           // [2 * pairs] shift of zs per run: written by pass X, read by pass Z
   float* shift_b;           // [2 * pairs] phi at site 0 of each run: written by pass Z, read by pass X
+  int* grid_out;            // host: receives the grid of a streamed pass (or null)
   DevScalars* sc;
   RedBuf rb;
 };
@@ -137,6 +138,19 @@ inline int launch_sep_runs(const SepArgs& a, int n, int axis, cudaStream_t s) {
   }
 }
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s);
+// Partials of the streamed passes of one kick in the reduction buffer: pass X
+// [grid][pe, GEx, sum phi_A, sum phi_B] at SEP_PART_X, pass Y [grid][GEy],
+// pass Z [grid][GEz, sum pi^2]; completed after pass Z by launch_sep_finalize.
+constexpr int SEP_PART_X = 0, SEP_PART_Y = 8192, SEP_PART_Z = 12288;
+struct SepFinArgs {
+  DevScalars* sc;
+  const double* part;  // the reduction buffer
+  int gx, gy, gz;      // blocks of the three passes
+  double hk, hg, hd;   // the kick, its grav-kinetic halves and the drift of pass X
+  double Nd;
+  int conf;
+};
+int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s);
 int sep_columns_16(int precision, int nf);
 int sep_columns_32(int precision, int nf);
 int sep_columns_64(int precision, int nf);

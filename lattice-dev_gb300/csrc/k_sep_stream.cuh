@@ -17,6 +17,10 @@
 // per line and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
 // needs ck before it has seen all momenta, so sum pi^2 comes from the pass Z
 // of the previous kick (or one reduction before the first pass X of a call).
+// The passes only write per-block partial sums; one single-block kernel after
+// pass Z (launch_sep_finalize) completes them in block order and advances
+// the scale factor, so no pass ends on a grid-wide arrival counter and the
+// scalar block holds the pre-kick state for all three passes.
 // Two fields use the lattice means as shifts; pairs of runs (Minkowski) use
 // each run's phi at site 0 as it was after the previous kick.
 //
@@ -45,7 +49,9 @@ template <int K> __device__ __forceinline__ void cp_wait_keep() {
 // table when P == Q), fk[k] = (f dk)^2 for wavenumber index k.  Every table
 // read is the thread's base plus a compile-time offset.  WARP: the P threads
 // of every line sit in one warp, so the transposes need only warp barriers.
-template <int N, bool WARP, typename Acc>
+// GE: add the axis' Parseval sum (f dk)^2 |Z_k|^2 / N to `ge` (only an
+// expanding background needs it).
+template <int N, bool WARP, bool GE, typename Acc>
 __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im)[Split<N>::Q], int t, float2* sl,
                                             const float2* tf, const float2* ti, const float* fk, Acc& ge) {
   constexpr int P = Split<N>::P, Q = Split<N>::Q, G = Q / P, S = P + 1;
@@ -75,17 +81,17 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
     }
     dft<P, false, float>(ur[g], ui[g]);
     const float* fkk = fk + kq;  // k = kq + Q kp
-    float gpart = 0.f;
+    float gp[4] = {0.f, 0.f, 0.f, 0.f};  // four independent partial sums
 #pragma unroll
     for (int kp = 0; kp < P; ++kp) {
       const float f2 = fkk[Q * kp];
       const float zr = ur[g][kp], zi = ui[g][kp];
-      gpart += f2 * (zr * zr + zi * zi);
+      if (GE) gp[kp % 4] += f2 * (zr * zr + zi * zi);
       const float h = -f2 * (1.0f / N);
       ur[g][kp] = zr * h;
       ui[g][kp] = zi * h;
     }
-    ge.add(gpart * (1.0f / N));
+    if (GE) ge.add(((gp[0] + gp[1]) + (gp[2] + gp[3])) * (1.0f / N));
     dft<P, true, float>(ur[g], ui[g]);
   }
   sync();
@@ -221,7 +227,7 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
 }
 
 // Pass X: drift, zs and the x part of the kick.
-template <int N, bool RUNS>
+template <int N, bool RUNS, bool CONF>
 __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     sep_stream_x(const __grid_constant__ SepArgs a) {
   using T = STile<0, N>;
@@ -247,19 +253,19 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   float* __restrict__ zs_o = static_cast<float*>(a.lap_out);
   const DevScalars* sc = a.sc;
-  double shAd = 0.0, shBd = 0.0;
+  // the FP64 scalars are read again by the last block (nothing writes them
+  // before it), so only the FP32 coefficients live through the tile loop
+  float shAf = 0.f, shBf = 0.f;
   if (!RUNS) {
-    shAd = __ldcg(&sc->mean[0]);
-    shBd = __ldcg(&sc->mean[1]);
+    shAf = (float)__ldcg(&sc->mean[0]);
+    shBf = (float)__ldcg(&sc->mean[1]);
   }
   const bool drift = a.hd != 0.0;
-  double a0 = 1.0, ap0 = 0.0, ke = 0.0;
   float cd = (float)a.hd, ck = (float)a.hk;
-  if (!RUNS && a.conf) {
-    a0 = __ldcg(&sc->a);
-    ke = __ldcg(&sc->ke_cur);
-    ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
-    const double a1 = a0 - a.hg * ap0 / 6.0;                     // Hamiltonian_grav_kinetic
+  if (CONF) {
+    const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
+    const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
+    const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
     cd = (float)(a.hd / (a0 * a0));
     ck = (float)(a.hk * a1 * a1);
   }
@@ -278,7 +284,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     const int64_t l0 = ((int64_t)blockIdx.x + j * gridDim.x) * LINES;
     const int64_t offA = tile_base<0>(a, l0 + li, pair);
     const int64_t offB = Nsite + offA;
-    float shA = (float)shAd, shB = (float)shBd;
+    float shA = shAf, shB = shBf;
     if (RUNS) {
       shA = nshA;
       shB = nshB;
@@ -295,7 +301,8 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     cp_wait_keep<0>();
     __syncwarp();
     float vr[Q], vi[Q], pA[Q], pB[Q];
-    float pes = 0.f, mAs = 0.f, mBs = 0.f;  // this line's sums, folded into KSum once
+    // this line's sums in four independent partials each, folded into KSum once
+    float pes[4] = {0.f, 0.f, 0.f, 0.f}, mAs[4] = {0.f, 0.f, 0.f, 0.f}, mBs[4] = {0.f, 0.f, 0.f, 0.f};
     const float* row = es + li * T::RS;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -313,12 +320,12 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       phic_o[offA + pos] = cA;
       phic_o[offB + pos] = cB;
       if (!RUNS) {
-        if (a.conf) {
+        if (CONF) {
           float ff[2] = {fA, fB};
-          pes += model_v<float, 2>(a.model, ff);
+          pes[q % 4] += model_v<float, 2>(a.model, ff);
         }
-        mAs += fA;
-        mBs += fB;
+        mAs[q % 4] += fA;
+        mBs[q % 4] += fB;
       }
       vr[q] = (fA - shA) - cA;
       vi[q] = (fB - shB) - cB;
@@ -326,14 +333,14 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       zs_o[offB + pos] = vi[q];
     }
     if (!RUNS) {
-      pe.add(pes);
-      mA.add(mAs);
-      mB.add(mBs);
+      pe.add((pes[0] + pes[1]) + (pes[2] + pes[3]));
+      mA.add((mAs[0] + mAs[1]) + (mAs[2] + mAs[3]));
+      mB.add((mBs[0] + mBs[1]) + (mBs[2] + mBs[3]));
     }
     __syncwarp();  // the warp's rows are free: stage its rows of the next tile
     if (j + 1 < my) stage_rows_x<N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, warp, lane);
     cp_commit();
-    d2_line_tab<N, true>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
+    d2_line_tab<N, true, CONF>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
@@ -343,26 +350,14 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   }
   cp_wait_all();
   if (RUNS) return;
-  double vals[4] = {pe.val(), ge.val(), mA.val(), mB.val()}, tot[4];
-  if (grid_reduce<4>(vals, a.rb, tot)) {
-    DevScalars* w = a.sc;
-    if (a.conf) {
-      w->ap = ap0;
-      w->pe = tot[0] / a.Nd;
-      if (drift) w->ke2 = ke;
-    }
-    w->gsum[0] = tot[1];
-    w->zsh[0] = shAd;
-    w->zsh[1] = shBd;
-    w->mean[0] = tot[2] / a.Nd;
-    w->mean[1] = tot[3] / a.Nd;
-    if (bad(tot[0]) || bad(tot[1])) w->err |= 1u;
-  }
+  // this block's sums; launch_sep_finalize completes them after pass Z
+  const double vals[4] = {pe.val(), ge.val(), mA.val(), mB.val()};
+  block_partials<4>(vals, a.rb.partials + SEP_PART_X);
 }
 
 // Passes Y (AXIS 1) and Z (AXIS 2): the y part of the kick; the z part with
 // the potential force, which completes the kick and its ysclp update.
-template <int AXIS, int N, bool RUNS>
+template <int AXIS, int N, bool RUNS, bool CONF>
 __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     sep_stream_yz(const __grid_constant__ SepArgs a) {
   using T = STile<AXIS, N>;
@@ -388,17 +383,19 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   const int64_t st = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   const DevScalars* sc = a.sc;
+  // the scalar block holds the state before this kick's pass X until
+  // launch_sep_finalize runs after pass Z: the shift pass X took (the means)
+  // and, from a, ysclp and sum pi^2, the same coefficients pass X computed
   float zshA = 0.f, zshB = 0.f;
   if (!RUNS && AXIS == 2) {
-    zshA = (float)__ldcg(&sc->zsh[0]);
-    zshB = (float)__ldcg(&sc->zsh[1]);
+    zshA = (float)__ldcg(&sc->mean[0]);
+    zshB = (float)__ldcg(&sc->mean[1]);
   }
-  double a0 = 1.0, ap0 = 0.0, a1 = 1.0;
   float ck = (float)a.hk, cv = (float)a.hk;
-  if (!RUNS && a.conf) {
-    a0 = __ldcg(&sc->a);
-    ap0 = __ldcg(&sc->ap);
-    a1 = a0 - a.hg * ap0 / 6.0;  // Hamiltonian_grav_kinetic before the kick
+  if (CONF) {
+    const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
+    const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // pass X's drift
+    const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
     ck = (float)(a.hk * a1 * a1);
     cv = (float)(a.hk * a1 * a1 * a1 * a1);
   }
@@ -446,10 +443,10 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     __syncthreads();
     if (j + 1 < my) stage_load<AXIS, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
     cp_commit();
-    d2_line_tab<N, false>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
+    d2_line_tab<N, false, CONF>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
     cp_wait_keep<1>();  // the momenta of this tile
     __syncthreads();
-    float kes = 0.f;
+    float kes[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
@@ -474,33 +471,24 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
         }
         pA = pA + (ck * vr[q] - cv * dA);
         pB = pB + (ck * vi[q] - cv * dB);
-        if (!RUNS) kes += pA * pA + pB * pB;
+        if (CONF) kes[q % 4] += pA * pA + pB * pB;
       }
       pi_o[sA] = pA;
       pi_o[sB] = pB;
     }
-    if (AXIS == 2 && !RUNS) ke.add(kes);
+    if (AXIS == 2 && CONF) ke.add((kes[0] + kes[1]) + (kes[2] + kes[3]));
     __syncthreads();
     if (j + 1 < my) stage_load<AXIS, N>(a, ls, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 1, tid);
     cp_commit();
   }
   cp_wait_all();
-  if (RUNS || !a.conf) return;
+  if constexpr (!CONF) return;
   if constexpr (AXIS == 1) {
-    double vals[1] = {ge.val()}, tot[1];
-    if (grid_reduce<1>(vals, a.rb, tot)) a.sc->gsum[1] = tot[0];
+    const double vals[1] = {ge.val()};
+    block_partials<1>(vals, a.rb.partials + SEP_PART_Y);
   } else {
-    double vals[2] = {ge.val(), ke.val()}, tot[2];
-    if (grid_reduce<2>(vals, a.rb, tot)) {
-      DevScalars* w = a.sc;
-      const double GE2 = (w->gsum[0] + w->gsum[1] + tot[0]) / (a1 * a1) / a.Nd;
-      const double ap1 = ap0 - a1 * a1 * a1 * (GE2 + 4.0 * w->pe) * a.hk;  // the kick's ysclp update
-      w->gsum[2] = tot[0];
-      w->ap = ap1;
-      w->a = a1 - a.hg * ap1 / 6.0;  // second Hamiltonian_grav_kinetic
-      w->ke_cur = tot[1];            // sum pi^2 for the next pass X
-      if (bad(GE2) || bad(tot[1])) w->err |= 1u;
-    }
+    const double vals[2] = {ge.val(), ke.val()};
+    block_partials<2>(vals, a.rb.partials + SEP_PART_Z);
   }
 }
 
@@ -510,6 +498,7 @@ int stream_launch(K k, int smem, int threads, int minb, int64_t ntiles, const Se
   if (e != cudaSuccess) return cuda_fail(e, "streamed separable pass smem attribute");
   const int64_t cap = (int64_t)minb * a.nsm;
   const int grid = (int)(ntiles < cap ? ntiles : cap);
+  if (a.grid_out) *a.grid_out = grid;  // host side: the blocks whose partials the finalize sums
   k<<<grid, threads, smem, s>>>(a);
   if (g_launch_counter) ++*g_launch_counter;
   e = cudaGetLastError();
@@ -531,12 +520,26 @@ int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
       (RUNS && (a.conf || !a.shift_a || !a.shift_b)))
     return set_error(LAT_ERR_STATE, "streamed separable pass: lines do not form whole tiles");
   const int64_t ntiles = a.nlines / lines;
+  // an expanding background (two fields only) adds the lattice sums of the
+  // Friedmann update; a static one needs none of them
+  if constexpr (!RUNS) {
+    if (a.conf) {
+      switch (axis) {
+        case 0: return stream_launch(sep_stream_x<N, false, true>, STile<0, N>::SMEM, STile<0, N>::THREADS,
+                                     STile<0, N>::MINB, ntiles, a, s);
+        case 1: return stream_launch(sep_stream_yz<1, N, false, true>, STile<1, N>::SMEM, STile<1, N>::THREADS,
+                                     STile<1, N>::MINB, ntiles, a, s);
+        default: return stream_launch(sep_stream_yz<2, N, false, true>, STile<2, N>::SMEM, STile<2, N>::THREADS,
+                                      STile<2, N>::MINB, ntiles, a, s);
+      }
+    }
+  }
   switch (axis) {
-    case 0: return stream_launch(sep_stream_x<N, RUNS>, STile<0, N>::SMEM, STile<0, N>::THREADS,
+    case 0: return stream_launch(sep_stream_x<N, RUNS, false>, STile<0, N>::SMEM, STile<0, N>::THREADS,
                                  STile<0, N>::MINB, ntiles, a, s);
-    case 1: return stream_launch(sep_stream_yz<1, N, RUNS>, STile<1, N>::SMEM, STile<1, N>::THREADS,
+    case 1: return stream_launch(sep_stream_yz<1, N, RUNS, false>, STile<1, N>::SMEM, STile<1, N>::THREADS,
                                  STile<1, N>::MINB, ntiles, a, s);
-    default: return stream_launch(sep_stream_yz<2, N, RUNS>, STile<2, N>::SMEM, STile<2, N>::THREADS,
+    default: return stream_launch(sep_stream_yz<2, N, RUNS, false>, STile<2, N>::SMEM, STile<2, N>::THREADS,
                                   STile<2, N>::MINB, ntiles, a, s);
   }
 }

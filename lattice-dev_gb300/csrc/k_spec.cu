@@ -291,6 +291,65 @@ int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "kmul launch");
 }
 
+// One block: the lattice sums of a kick of the streamed separable passes in
+// block order, then the scalar chain of the kick (hamiltonian_conformal.f90:
+// 86-174): the drift's ysclp += hd KE2/a^3, a1 = a - hg ysclp/6, the kick's
+// ysclp -= a1^3 (GE2/a1^2 + 4 PE) hk, a = a1 - hg ysclp/6; and the lattice
+// means, the shifts of the next kick.
+__global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
+  __shared__ double sh[8][32];
+  __shared__ double tot[8];
+  const int nv[3] = {4, 1, 2}, nb[3] = {f.gx, f.gy, f.gz}, off[3] = {SEP_PART_X, SEP_PART_Y, SEP_PART_Z};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int k = 0;
+  for (int p = 0; p < 3; ++p)
+    for (int i = 0; i < nv[p]; ++i, ++k) {
+      double x = 0.0;
+      for (int b = threadIdx.x; b < nb[p]; b += blockDim.x) x += f.part[off[p] + (size_t)b * nv[p] + i];
+      x = warp_sum(x);
+      if (lane == 0) sh[k][wid] = x;
+    }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += sh[threadIdx.x][w];
+    tot[threadIdx.x] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  // tot: pe, GEx, sum phi_A, sum phi_B, GEy, GEz, sum pi^2
+  DevScalars* w = f.sc;
+  w->zsh[0] = w->mean[0];  // the shift this kick's zs was taken with
+  w->zsh[1] = w->mean[1];
+  w->mean[0] = tot[2] / f.Nd;
+  w->mean[1] = tot[3] / f.Nd;
+  w->gsum[0] = tot[1];
+  w->gsum[1] = tot[4];
+  w->gsum[2] = tot[5];
+  if (f.conf) {
+    const double a0 = w->a, ke = w->ke_cur;
+    const double ap0 = w->ap + f.hd * (ke / f.Nd) / (a0 * a0 * a0);
+    const double a1 = a0 - f.hg * ap0 / 6.0;
+    const double GE2 = (tot[1] + tot[4] + tot[5]) / (a1 * a1) / f.Nd;
+    const double PE = tot[0] / f.Nd;
+    const double ap1 = ap0 - a1 * a1 * a1 * (GE2 + 4.0 * PE) * f.hk;
+    w->pe = PE;
+    if (f.hd != 0.0) w->ke2 = ke;
+    w->ap = ap1;
+    w->a = a1 - f.hg * ap1 / 6.0;
+    w->ke_cur = tot[6];
+    if (bad(PE) || bad(GE2) || bad(tot[6])) w->err |= 1u;
+  }
+  if (bad(tot[2]) || bad(tot[3])) w->err |= 1u;
+}
+
+int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s) {
+  sep_finalize_kernel<<<1, 256, 0, s>>>(f);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "separable finalize launch");
+}
+
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s) {
   if (n % 4) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
   pi2_kernel<<<grid, 256, 0, s>>>(static_cast<const float4*>(pi), n / 4, sc, rb);
