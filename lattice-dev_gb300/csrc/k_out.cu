@@ -223,7 +223,43 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
   using Acc = typename AccOf<R>::type;
   Acc s[8];
   const R c0 = (R)a.c[0], c1 = (R)a.c[1], c2 = (R)a.c[2], c3 = (R)a.c[3];
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+  int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (sizeof(R) == 4) {
+    // spectral, no GW arrays: four sites per thread and step (float4 loads),
+    // one compensated add per sum and four sites
+    if (!a.fd && !u && N % 4 == 0) {  // every field's array starts 16-byte aligned
+      const int64_t n4 = N / 4;
+      for (int64_t v = t0; v < n4; v += (int64_t)gridDim.x * blockDim.x) {
+        float4 fq[NF], pq[NF];
+#pragma unroll
+        for (int l = 0; l < NF; ++l) {
+          fq[l] = __ldcs(reinterpret_cast<const float4*>(phi + l * N) + v);
+          pq[l] = __ldcs(reinterpret_cast<const float4*>(pi + l * N) + v);
+        }
+        R ke = 0, pe = 0, m0 = 0, m1 = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          R f[NF];
+#pragma unroll
+          for (int l = 0; l < NF; ++l) {
+            const float4 F4 = fq[l], P4 = pq[l];
+            f[l] = j == 0 ? F4.x : (j == 1 ? F4.y : (j == 2 ? F4.z : F4.w));
+            const R p = j == 0 ? P4.x : (j == 1 ? P4.y : (j == 2 ? P4.z : P4.w));
+            ke += p * p;
+          }
+          pe += model_v<R, NF>(a.model, f);
+          m0 += f[0];
+          if (NF > 1) m1 += f[NF > 1 ? 1 : 0];
+        }
+        s[0].add(ke);
+        s[1].add(pe);
+        s[2].add(m0);
+        if (NF > 1) s[3].add(m1);
+      }
+      t0 = N;  // no tail
+    }
+  }
+  for (int64_t t = t0; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     R f[NF];
 #pragma unroll
     for (int l = 0; l < NF; ++l) {
@@ -286,25 +322,35 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
   }
 }
 
+// sum over the half spectra of all fields of w k^2 |F_k|^2 (w = 2 for the
+// modes whose conjugate partner is not stored): one warp per row (y, z,
+// field) of nx/2+1 modes, the row's y and z part of k^2 computed once, the
+// terms in the field precision, compensated sums per lane.
 template <typename R, typename C>
 __global__ void __launch_bounds__(256) parseval_kernel(const C* F, int nx, int ny, int nz, int nf, double dkx2,
                                                        double dky2, double dkz2, DevScalars* sc, int slot,
                                                        RedBuf rb) {
-  const unsigned int hx = nx / 2 + 1;
-  const unsigned int M = hx * (unsigned int)ny * (unsigned int)nz;
-  double acc = 0.0;
-  for (unsigned int m = blockIdx.x * blockDim.x + threadIdx.x; m < M * (unsigned int)nf; m += gridDim.x * blockDim.x) {
-    const unsigned int mm = m % M;
-    const int x = (int)(mm % hx);
-    const unsigned int r = mm / hx;
-    const int y = (int)(r % (unsigned int)ny), z = (int)(r / (unsigned int)ny);
+  const int hx = nx / 2 + 1;
+  const int64_t rows = (int64_t)ny * nz * nf;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  using Acc = typename AccOf<R>::type;
+  Acc acc;
+  for (int64_t row = warp0; row < rows; row += nwarps) {
+    const int64_t rr = row % ((int64_t)ny * nz);
+    const int y = (int)(rr % ny), z = (int)(rr / ny);
     const int jj = fold_idx(y, ny), kk = fold_idx(z, nz);
-    const double k2 = (double)(x * x) * dkx2 + (double)(jj * jj) * dky2 + (double)(kk * kk) * dkz2;
-    const double w = (x == 0 || 2 * x == nx) ? 1.0 : 2.0;
-    const C v = F[m];
-    acc += w * k2 * ((double)v.x * v.x + (double)v.y * v.y);
+    const R kyz = (R)((double)(jj * jj) * dky2 + (double)(kk * kk) * dkz2);
+    const C* Fr = F + row * hx;
+    for (int x = lane; x < hx; x += 32) {
+      const C v = Fr[x];
+      const R w = (x == 0 || 2 * x == nx) ? R(1) : R(2);
+      const R k2 = (R)(x * x) * (R)dkx2 + kyz;
+      acc.add(w * k2 * (v.x * v.x + v.y * v.y));
+    }
   }
-  double vv[1] = {acc}, t[1];
+  double vv[1] = {acc.val()}, t[1];
   if (grid_reduce<1>(vv, rb, t)) sc->red[slot] = t[0];
 }
 
