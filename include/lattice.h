@@ -281,6 +281,15 @@ int lat_write_energy_line(lat_t* h, const char* path, double time);
  * spectrum, then zeros up to 2 nfld + 2 columns (columns the reference
  * leaves unset), then an empty line. */
 int lat_write_spectrum_block(lat_t* h, const char* path);
+/* output_cube (Discrete/Bubble-Collisions/outputfile.f90:942-1016): writes
+ * every ds-th site of field `field` (what = LAT_SPEC_FLD) or of its momentum
+ * (LAT_SPEC_FLDP) as FP64 little-endian, x fastest, to
+ * <dir>/<name>-<frame, 5 digits>.raw, and the VisIt brick-of-values header
+ * <dir>/<name>-<frame>.bov (TIME, VARIABLE, BRICK_ORIGIN, BRICK_SIZE = n dx,
+ * DATA_FILE, DATA_SIZE = n / ds, DATA_FORMAT DOUBLE, DATA_ENDIAN LITTLE,
+ * CENTERING zonal).  Every side must be a multiple of ds. */
+int lat_write_cube(lat_t* h, int32_t what, int32_t field, int32_t ds, const char* dir, const char* name,
+                   int32_t frame, double time);
 
 /* ------------------------------------------------------------- ensembles */
 /* A batch of independent runs of one model on lattices of uneven size,

@@ -120,6 +120,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_device_ptr": ([P, I, C.POINTER(P)], I), "lat_host_alloc": ([C.POINTER(P), C.c_size_t], I),
         "lat_host_free": ([P], I), "lat_autotune": ([P, C.c_char_p], I),
         "lat_tuning_get": ([P, C.POINTER(I)], I), "lat_sep_streamed": ([P, C.POINTER(I)], I),
+        "lat_write_cube": ([P, I, I, I, C.c_char_p, C.c_char_p, I, C.c_double], I),
         "lat_dev_alloc": ([I, C.POINTER(P), C.c_size_t], I), "lat_dev_free": ([P], I),
         "lat_memcpy": ([P, P, C.c_size_t, I], I),
         "lat_net_nparams": ([], I64), "lat_net_create": ([C.POINTER(P), I, U64], I), "lat_net_destroy": ([P], I),
@@ -398,6 +399,10 @@ class Lattice:
         return bool(on.value)
 
     # output files in the reference's column layouts
+    def write_cube(self, what: int, field: int, ds: int, directory, name: str, frame: int, time: float) -> None:
+        """output_cube: <directory>/<name>-<frame>.raw (FP64, every ds-th site) and the .bov header."""
+        _check(_lib.lat_write_cube(self._h, what, field, ds, str(directory).encode(), name.encode(), frame, time))
+
     def write_energy_line(self, path, time: float) -> None:
         _check(_lib.lat_write_energy_line(self._h, str(path).encode(), time))
 

@@ -1983,6 +1983,48 @@ int lat_write_spectrum_block(lat_t* h, const char* path) {
   return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);
 }
 
+int lat_write_cube(lat_t* h, int32_t what, int32_t field, int32_t ds, const char* dir, const char* name,
+                   int32_t frame, double time) {
+  if (!h || !dir || !name) return set_error(LAT_ERR_ARG, "null argument");
+  if (ds < 1 || h->nx % ds || h->ny % ds || h->nz % ds) return set_error(LAT_ERR_ARG, "sides must be multiples of ds");
+  if (frame < 0 || frame > 99999) return set_error(LAT_ERR_ARG, "frame: 0..99999");
+  ApiGuard g(h);
+  const void* src = nullptr;
+  RET(src_ptr(h, what, field, &src));
+  const void* c = nullptr;
+  if (what == LAT_SPEC_FLD && h->prec == LAT_FP32_KAHAN)
+    c = (const char*)h->fldc + (size_t)field * h->N * h->rsz;
+  const int mx = h->nx / ds, my = h->ny / ds, mz = h->nz / ds;
+  const size_t M = (size_t)mx * my * mz;
+  RET(ensure_stage(h, M));
+  RET(launch_cube(src, c, h->nx, h->ny, h->nz, ds, h->prec, h->stage, h->stream));
+  std::vector<double> buf(M);
+  CK(cudaMemcpyAsync(buf.data(), h->stage, M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  char base[64];
+  snprintf(base, sizeof(base), "-%05d", (int)frame);
+  const std::string raw_name = std::string(name) + base + ".raw";
+  const std::string raw = std::string(dir) + "/" + raw_name;
+  const std::string bov = std::string(dir) + "/" + name + base + ".bov";
+  FILE* fp = fopen(raw.c_str(), "wb");
+  if (!fp) return set_error(LAT_ERR_IO, "cannot open " + raw);
+  const bool okr = fwrite(buf.data(), sizeof(double), M, fp) == M;
+  if (fclose(fp) != 0 || !okr) return set_error(LAT_ERR_IO, "write failed: " + raw);
+  fp = fopen(bov.c_str(), "w");
+  if (!fp) return set_error(LAT_ERR_IO, "cannot open " + bov);
+  fprintf(fp, "TIME:        %25.16E\n", time);
+  fprintf(fp, "VARIABLE:    %s\n", name);
+  fprintf(fp, "BRICK_ORIGIN:%25.16E%25.16E%25.16E\n", 0.0, 0.0, 0.0);
+  fprintf(fp, "BRICK_SIZE:  %25.16E%25.16E%25.16E\n", h->nx * h->dx, h->ny * h->dx, h->nz * h->dx);
+  fprintf(fp, "DATA_FILE:   %s\n", raw_name.c_str());
+  fprintf(fp, "DATA_SIZE:   %5d%5d%5d\n", mx, my, mz);
+  fprintf(fp, "DATA_FORMAT: DOUBLE\n");
+  fprintf(fp, "DATA_ENDIAN: LITTLE\n");
+  fprintf(fp, "CENTERING:   zonal\n");
+  if (fclose(fp) != 0) return set_error(LAT_ERR_IO, "write failed: " + bov);
+  return LAT_OK;
+}
+
 int lat_sep_streamed(const lat_t* h, int32_t* on) {
   if (!h || !on) return set_error(LAT_ERR_ARG, "null argument");
   *on = h->sep_ok && h->sep_stream ? 1 : 0;

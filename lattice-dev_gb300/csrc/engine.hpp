@@ -179,6 +179,8 @@ int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi
 int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos,
                    cudaStream_t s);
 int launch_to_fp64(const void* hi, const void* c, int64_t n, int precision, double* out, cudaStream_t s);
+int launch_cube(const void* hi, const void* c, int nx, int ny, int nz, int ds, int precision, double* out,
+                cudaStream_t s);
 int launch_from_fp64(const double* in, int64_t n, int precision, void* hi, void* c, cudaStream_t s);
 
 struct SpecArgs {

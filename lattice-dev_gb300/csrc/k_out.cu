@@ -497,6 +497,33 @@ int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precisi
   else soa2aos_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>((const float*)hi, (const float*)c, nf, N, aos);
   return done("soa2aos");
 }
+// Every ds-th site of one field array as FP64 (phi_hi - c for FP32), in the
+// lattice order (x fastest): the data of output_cube
+// (Discrete/Bubble-Collisions/outputfile.f90:942-1016).
+template <typename R, bool KAHAN>
+__global__ void cube_kernel(const R* __restrict__ hi, const R* __restrict__ c, int nx, int ny, int nz, int ds,
+                            double* __restrict__ out) {
+  const int mx = nx / ds, my = ny / ds, mz = nz / ds;
+  const int64_t M = (int64_t)mx * my * mz;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < M; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % mx), j = (int)((o / mx) % my), k = (int)(o / ((int64_t)mx * my));
+    const int64_t s = ((int64_t)k * ds * ny + (int64_t)j * ds) * nx + (int64_t)i * ds;
+    out[o] = KAHAN ? (double)hi[s] - (double)c[s] : (double)hi[s];
+  }
+}
+
+int launch_cube(const void* hi, const void* c, int nx, int ny, int nz, int ds, int precision, double* out,
+                cudaStream_t s) {
+  const int64_t M = (int64_t)(nx / ds) * (ny / ds) * (nz / ds);
+  if (precision == LAT_FP64)
+    cube_kernel<double, false><<<grid_for(M), 256, 0, s>>>((const double*)hi, nullptr, nx, ny, nz, ds, out);
+  else if (c)
+    cube_kernel<float, true><<<grid_for(M), 256, 0, s>>>((const float*)hi, (const float*)c, nx, ny, nz, ds, out);
+  else
+    cube_kernel<float, false><<<grid_for(M), 256, 0, s>>>((const float*)hi, nullptr, nx, ny, nz, ds, out);
+  return done("cube");
+}
+
 int launch_to_fp64(const void* hi, const void* c, int64_t n, int precision, double* out, cudaStream_t s) {
   if (precision == LAT_FP64) to64_kernel<double, false><<<grid_for(n), 256, 0, s>>>((const double*)hi, nullptr, n, out);
   else to64_kernel<float, true><<<grid_for(n), 256, 0, s>>>((const float*)hi, (const float*)c, n, out);

@@ -368,6 +368,31 @@ def test_prepared_graph_leaves_state_and_replays(engine):
     assert out[0][1] == out[1][1]
 
 
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32_KAHAN])
+def test_output_cube_bov(engine, tmp_path, prec):
+    """output_cube's brick of values: every ds-th site as FP64, x fastest,
+    and the .bov header VisIt reads (outputfile.f90:942-1016)."""
+    c = L.make_config((16, 8, 12), nfld=2, length=8.0, laplacian=L.LAP_FD27, precision=prec,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g = engine.Lattice(c)
+    f, p = random_state((2, 12, 8, 16), seed=41, mean=0.3, amp=0.1)
+    g.set_state(f, p)
+    gf, gp = g.get_state()
+    for what, field, ds, arr in ((L.SPEC_FLD, 1, 2, gf), (L.SPEC_FLDP, 0, 4, gp), (L.SPEC_FLD, 0, 1, gf)):
+        g.write_cube(what, field, ds, tmp_path, "fld", 7 + ds, 1.25)
+        raw = np.fromfile(tmp_path / f"fld-{7 + ds:05d}.raw", dtype="<f8")
+        want = arr[field][::ds, ::ds, ::ds]
+        assert raw.size == want.size and np.array_equal(raw.reshape(want.shape), want)
+        hdr = dict(ln.split(":", 1) for ln in (tmp_path / f"fld-{7 + ds:05d}.bov").read_text().splitlines())
+        assert float(hdr["TIME"]) == 1.25 and hdr["VARIABLE"].strip() == "fld"
+        assert [float(x) for x in hdr["BRICK_SIZE"].split()] == [8.0, 4.0, 6.0]
+        assert [int(x) for x in hdr["DATA_SIZE"].split()] == [16 // ds, 8 // ds, 12 // ds]
+        assert hdr["DATA_FILE"].strip() == f"fld-{7 + ds:05d}.raw"
+        assert hdr["DATA_FORMAT"].strip() == "DOUBLE" and hdr["CENTERING"].strip() == "zonal"
+    with pytest.raises(engine.LatticeError):
+        g.write_cube(L.SPEC_FLD, 0, 3, tmp_path, "fld", 1, 0.0)  # 16 is not a multiple of 3
+
+
 def test_output_files_reference_layout(engine, tmp_path):
     """energy_spec.out and spectrum.out records in the reference's column
     layout (ES22.15 + 2X fields), with the values of the engine's reductions."""
