@@ -297,23 +297,28 @@ int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
 // ysclp -= a1^3 (GE2/a1^2 + 4 PE) hk, a = a1 - hg ysclp/6; and the lattice
 // means, the shifts of the next kick.
 __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
-  __shared__ double sh[8][32];
+  // warp w < 7 sums value w of the seven (pass X: pe, GEx, sum phi_A, sum
+  // phi_B; Y: GEy; Z: GEz, sum pi^2) over the blocks, all loads of a lane in
+  // flight at once; the order of every sum is fixed
   __shared__ double tot[8];
-  const int nv[3] = {4, 1, 2}, nb[3] = {f.gx, f.gy, f.gz}, off[3] = {SEP_PART_X, SEP_PART_Y, SEP_PART_Z};
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int k = 0;
-  for (int p = 0; p < 3; ++p)
-    for (int i = 0; i < nv[p]; ++i, ++k) {
-      double x = 0.0;
-      for (int b = threadIdx.x; b < nb[p]; b += blockDim.x) x += f.part[off[p] + (size_t)b * nv[p] + i];
-      x = warp_sum(x);
-      if (lane == 0) sh[k][wid] = x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (wid < 7) {
+    const int p = wid < 4 ? 0 : (wid == 4 ? 1 : 2);
+    const int nv = p == 0 ? 4 : (p == 1 ? 1 : 2), i = p == 0 ? wid : (p == 1 ? 0 : wid - 5);
+    const int nb = p == 0 ? f.gx : (p == 1 ? f.gy : f.gz);
+    const double* src = f.part + (p == 0 ? SEP_PART_X : (p == 1 ? SEP_PART_Y : SEP_PART_Z)) + i;
+    double v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int b = lane + 32 * r;
+      v[r] = b < nb ? __ldcg(src + (size_t)b * nv) : 0.0;
     }
-  __syncthreads();
-  if (threadIdx.x < 7) {
-    double s = 0.0;
-    for (int w = 0; w < nw; ++w) s += sh[threadIdx.x][w];
-    tot[threadIdx.x] = s;
+    double x = 0.0;
+    for (int b = lane + 32 * 16; b < nb; b += 32) x += __ldcg(src + (size_t)b * nv);  // more than 512 blocks
+#pragma unroll
+    for (int r = 0; r < 16; ++r) x += v[r];
+    x = warp_sum(x);
+    if (lane == 0) tot[wid] = x;
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
