@@ -7,7 +7,7 @@
 // kick in this form, line A and line B forming one complex line:
 //
 //   pass X: drift of phi (Kahan), z = (phi - shift) - c written as the FP32
-//           array zs, pi += ck d2x(z)                       [PE, GEx, means]
+//           array zs (lines A and B interleaved), pi += ck d2x(z)  [PE, GEx, means]
 //   pass Y: pi += ck d2y(zs)                                 [GEy]
 //   pass Z: pi += ck d2z(zs) - cv V'(zs + shift)             [GEz, sum pi^2]
 //
@@ -142,7 +142,7 @@ struct STile {
   static constexpr int RS = AXIS == 0 ? N + P : LINES;
   static constexpr int ROWS = AXIS == 0 ? LINES : N;
   static constexpr int ARR = ROWS * RS;               // floats per staged array
-  static constexpr int N_EARLY = AXIS == 0 ? 6 : 2;   // X: phi, c, pi of both lines; Y, Z: zs
+  static constexpr int N_EARLY = AXIS == 0 ? 6 : 2;   // X: phi, c, pi of both lines; Y, Z: zs (float2 rows)
   static constexpr int N_LATE = AXIS == 0 ? 0 : 2;    // Y, Z: pi of both lines
   // transpose scratch per line, in complex: Q rows of P + 1, padded so the
   // lines a warp touches at once start in different banks
@@ -179,27 +179,41 @@ __device__ __forceinline__ int64_t tile_base(const SepArgs& a, int64_t l0, int64
   return pbase + (AXIS == 1 ? o * plane : o * a.nx) + x0;
 }
 
-// Passes Y, Z: copy the early (part 0: zs) or late (part 1: pi) inputs of
-// tile `tile`, both lines, into a slot with 16-byte cp.async copies.  Thread
-// tid copies chunk tid % CPR of rows tid / CPR + j * (THREADS / CPR).
+// Passes Y, Z: copy the early inputs (part 0: zs, both lines interleaved as
+// float2, one row of LINES float2 per position) or the late ones (part 1: pi
+// of line A and of line B, rows of LINES floats) of tile `tile` into a slot
+// with 16-byte cp.async copies.  Thread tid copies chunk tid % CPR of rows
+// tid / CPR + j * (THREADS / CPR).
 template <int AXIS, int N>
 __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t tile, int part, int tid) {
   using T = STile<AXIS, N>;
-  constexpr int CPR = T::RS / 4;  // 16-byte chunks per staged row
-  constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
-  static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
   const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
-  const int row0 = tid / CPR, ch = tid % CPR;
+  const int64_t stride = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
   int64_t pair;
   const int64_t base = tile_base<AXIS>(a, tile * T::LINES, pair);
-  const int64_t stride = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
-  const int64_t jstep = RPJ * stride;
-  float* d0 = dst + row0 * T::RS + ch * 4;
-  const float* src = static_cast<const float*>(part == 0 ? a.lap : a.pi) + base + row0 * stride + ch * 4;
+  if (part == 0) {
+    constexpr int CPR = T::RS / 2;  // 16-byte chunks (two float2) per staged row
+    constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
+    static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
+    const int row0 = tid / CPR, ch = tid % CPR;
+    // zs of the pair in float2 units: pair * Ns + the site offset within the pair
+    const float* src = static_cast<const float*>(a.lap) + 2 * (base - pair * Ns + row0 * stride) + ch * 4;
+    float* d0 = dst + row0 * 2 * T::RS + ch * 4;
 #pragma unroll
-  for (int f = 0; f < 2; ++f) {
+    for (int j = 0; j < STEPS; ++j) cp16(d0 + j * RPJ * 2 * T::RS, src + 2 * j * RPJ * stride);
+  } else {
+    constexpr int CPR = T::RS / 4;  // 16-byte chunks per staged row
+    constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
+    static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
+    const int row0 = tid / CPR, ch = tid % CPR;
+    const int64_t jstep = RPJ * stride;
+    float* d0 = dst + row0 * T::RS + ch * 4;
+    const float* src = static_cast<const float*>(a.pi) + base + row0 * stride + ch * 4;
 #pragma unroll
-    for (int j = 0; j < STEPS; ++j) cp16(d0 + f * T::ARR + j * RPJ * T::RS, src + f * Ns + j * jstep);
+    for (int f = 0; f < 2; ++f) {
+#pragma unroll
+      for (int j = 0; j < STEPS; ++j) cp16(d0 + f * T::ARR + j * RPJ * T::RS, src + f * Ns + j * jstep);
+    }
   }
 }
 
@@ -284,6 +298,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     const int64_t l0 = ((int64_t)blockIdx.x + j * gridDim.x) * LINES;
     const int64_t offA = tile_base<0>(a, l0 + li, pair);
     const int64_t offB = Nsite + offA;
+    float2* zs2 = reinterpret_cast<float2*>(zs_o) + (offA - pair * Nsite);  // both lines, interleaved
     float shA = shAf, shB = shBf;
     if (RUNS) {
       shA = nshA;
@@ -329,8 +344,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       }
       vr[q] = (fA - shA) - cA;
       vi[q] = (fB - shB) - cB;
-      zs_o[offA + pos] = vr[q];
-      zs_o[offB + pos] = vi[q];
+      zs2[pos] = make_float2(vr[q], vi[q]);
     }
     if (!RUNS) {
       pe.add((pes[0] + pes[1]) + (pes[2] + pes[3]));
@@ -426,8 +440,9 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
-      vr[q] = es[pos * T::RS + li];
-      vi[q] = es[T::ARR + pos * T::RS + li];
+      const float2 z = reinterpret_cast<const float2*>(es)[pos * T::RS + li];
+      vr[q] = z.x;
+      vi[q] = z.y;
       if constexpr (AXIS == 2) {
         hA[q] = vr[q] + zshA;  // phi - c
         hB[q] = vi[q] + zshB;
