@@ -247,3 +247,14 @@ def test_ensemble_streamed_passes(engine, monkeypatch):
         assert err_s <= 2 * err_c + 1e-5, (r, sizes[r], err_s, err_c)
         assert rel_err(s32[r][1], ref_p) <= 2e-4, r
         assert abs(E32[r, L.E_RHO] - E64[r, L.E_RHO]) <= 1e-5 * abs(E64[r, L.E_RHO])
+
+
+def test_ensemble_odd_class_keeps_cufft(engine):
+    """A size class with an odd number of runs cannot pair its runs: the
+    ensemble keeps per-class cuFFT for every class."""
+    base = L.make_config(16, nfld=1, length=20.0, laplacian=L.LAP_SPECTRAL, precision=L.FP32_KAHAN,
+                         model=L.MODEL_PHI4)
+    assert engine.Ensemble(base, [64, 64]).sep_streamed()
+    assert not engine.Ensemble(base, [64, 64, 64]).sep_streamed()
+    assert not engine.Ensemble(base, [64, 64, 96]).sep_streamed()
+    assert not engine.Ensemble(base, [48, 48]).sep_streamed()  # 48-point lines have no streamed pass
