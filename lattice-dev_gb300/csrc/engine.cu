@@ -992,7 +992,7 @@ int lat_create(lat_t** out, const lat_config* cfg) {
   h->pw_grid = h->nsm * 4;
   int64_t maxb = std::max<int64_t>(h->pw_grid, 4096);
   for (int ty : {2, 4, 8, 16})
-    for (int zc : {4, 8, 16, 32, 64}) maxb = std::max<int64_t>(maxb, fd_max_blocks(h->nx, h->ny, h->nz, ty, zc));
+    for (int zc : {2, 4, 8, 16, 32, 64}) maxb = std::max<int64_t>(maxb, fd_max_blocks(h->nx, h->ny, h->nz, ty, zc));
   h->red_cap = maxb;
   if ((st = alloc((void**)&h->rb.partials, (size_t)maxb * 16 * sizeof(double)))) return bail(st);
   if ((st = alloc((void**)&h->rb.counter, 64))) return bail(st);
@@ -1742,7 +1742,7 @@ int lat_autotune(lat_t* h, const char* cache_path) {
   const int reps = h->N >= (1 << 22) ? 3 : 10;
   if (!spectral(h)) {
     for (int ty : {2, 4, 8, 16})
-      for (int zc : {8, 16, 32, 64}) {
+      for (int zc : {2, 4, 8, 16, 32, 64}) {  // short z-chunks: enough blocks on small lattices
         if (st != LAT_OK) break;
         if (zc > h->nz && zc != 8) continue;
         h->fd_ty = ty;
