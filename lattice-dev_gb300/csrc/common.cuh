@@ -32,7 +32,7 @@ struct DevScalars {
   double red[16];  // raw sums of the last stand-alone reduction (energies)
   double gsum[3];  // -sum phi d2_axis(phi) of the separable passes X, Y, Z
   double mean[4];  // lattice means of the fields (spectral shift of the separable passes)
-  double zsh[2];   // shift of the zs array the last streamed pass X wrote (k_sep_stream.cuh)
+  double zsh[2];   // shift the zs array of the last streamed kick was taken with (k_sep_stream.cuh)
   double ke_cur;   // sum pi^2 of the current momenta, kept by the streamed passes
   unsigned int err;  // bit 0: NaN/Inf met in a reduction
   unsigned int pad[3];

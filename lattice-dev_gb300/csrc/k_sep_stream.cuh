@@ -157,8 +157,8 @@ struct STile {
   static constexpr int TI_OFF = P == Q ? TF_OFF : TF_OFF + 2 * N;
   static constexpr int FK_OFF = TI_OFF + 2 * N;                   // (f dk)^2
   static constexpr int SMEM = (FK_OFF + N) * 4;
-  // blocks per SM: dynamic and static (reduction) shared memory plus the
-  // 1 KB the SM reserves per block, within 228 KB; at most 3
+  // blocks per SM: dynamic and static (block partials) shared memory plus
+  // the 1 KB the SM reserves per block, within 228 KB; at most 3
   static constexpr int PER_BLOCK = SMEM + 1300 + 1024;
   static constexpr int MINB = (228 * 1024) / PER_BLOCK > 3 ? 3 : (228 * 1024) / PER_BLOCK;
   static_assert(MINB >= 1, "a block must fit in shared memory");
@@ -267,8 +267,8 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
   float* __restrict__ zs_o = static_cast<float*>(a.lap_out);
   const DevScalars* sc = a.sc;
-  // the FP64 scalars are read again by the last block (nothing writes them
-  // before it), so only the FP32 coefficients live through the tile loop
+  // the scalar block holds the pre-kick state until launch_sep_finalize runs
+  // after pass Z; only the FP32 coefficients live through the tile loop
   float shAf = 0.f, shBf = 0.f;
   if (!RUNS) {
     shAf = (float)__ldcg(&sc->mean[0]);
@@ -370,7 +370,8 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
 }
 
 // Passes Y (AXIS 1) and Z (AXIS 2): the y part of the kick; the z part with
-// the potential force, which completes the kick and its ysclp update.
+// the potential force, which completes the kick (its ysclp update follows in
+// launch_sep_finalize).
 template <int AXIS, int N, bool RUNS, bool CONF>
 __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     sep_stream_yz(const __grid_constant__ SepArgs a) {
