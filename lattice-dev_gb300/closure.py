@@ -99,6 +99,7 @@ def generate(s: Setup, seeds, t_start, t_end, n_snap, capacity=None, progress=No
     for seed in seeds:
         g = L.Lattice(s.config(s.n_fine, s.fine_precision))
         init_fine(s, g, seed)
+        g.autotune(None)
         done = 0
         for t in times:
             k = int(round(t / dt)) - done
@@ -196,6 +197,7 @@ def evaluate(s: Setup, net, seeds, t_eval, every=3, coarse_precision=L.FP32_KAHA
     for seed in seeds:
         f = L.Lattice(s.config(s.n_fine, s.fine_precision))
         init_fine(s, f, seed)
+        f.autotune(None)  # the fine reference runs on the engine's fastest path for its lattice
         fld0, mom0, _ = coarse_state(s, f, scratch)
         dtf = s.dt(s.n_fine)
         kf = int(round(t_eval / dtf))
