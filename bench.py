@@ -625,7 +625,7 @@ def conv_roofline(L, net, n, reps=10):
     out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                        "peak_kind": kind + " dense bf16 (cuBLAS burst)",
                        "note": "conv1 (4 padded to 8 -> 32) and conv2 (32->32) on tcgen05.mma with TMEM "
-                               "accumulators when nx % 128 == 0, conv3 (32->2) on mma.sync; BF16 in, FP32 accumulate"}
+                               "accumulators when nx % 64 == 0, conv3 (32->2) on mma.sync; BF16 in, FP32 accumulate"}
     return out
 
 

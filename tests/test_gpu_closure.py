@@ -39,9 +39,11 @@ def _net(engine, seed, scale_last=1.0):
     return net, q.astype(np.float64), norm
 
 
-# (16, 8, 4): every layer on the mma.sync kernels; (128, 8, 2): the 32 -> 32
-# layer (forward and backward data) on the tcgen05 / tensor-memory kernel
-SHAPES = [(16, 8, 4), (128, 8, 2)]
+# (16, 8, 4): every layer on the mma.sync kernels; (128, 8, 2) and (64, 8, 5):
+# the 4 -> 32 and 32 -> 32 layers (forward and backward data) on the tcgen05 /
+# tensor-memory kernel, with 128-site x-rows and with two 64-site x-rows per
+# M tile (five z-planes: one item's plane ring wraps)
+SHAPES = [(16, 8, 4), (128, 8, 2), (64, 8, 5)]
 
 
 @pytest.mark.parametrize("SHAPE", SHAPES)
