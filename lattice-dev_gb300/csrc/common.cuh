@@ -57,10 +57,40 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Compensated FP32 accumulator: per-thread partial sums stay in FP32 (GB300
-// runs FP64 at a small fraction of its FP32 rate) while keeping ~FP64
-// accuracy; the FP64 conversion happens once per thread.
+// Float-float value hi + lo: the warp-level partial sums of compensated FP32
+// accumulators.  GB300 runs FP64 at a small fraction of its FP32 rate, so a
+// warp's 31 additions run on the FP32 pipes (relative error ~2^-47) and only
+// the warp's total is converted to FP64.
+struct FF {
+  float hi, lo;
+};
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest, no reassociation)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bv = s - a;
+  e = (a - (s - bv)) + (b - bv);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e, hi, lo;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  two_sum(s, e, hi, lo);  // renormalise
+  return FF{hi, lo};
+}
+__device__ __forceinline__ double warp_sum(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const FF w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    v = ff_add(v, w);
+  }
+  return (double)v.hi + (double)v.lo;
+}
+
+// Compensated FP32 accumulator: per-thread partial sums stay in FP32 while
+// keeping ~FP64 accuracy; red() hands the sum s - c to the reductions as a
+// float-float value.
 struct KSum {
+  using Red = FF;
   float s = 0.f, c = 0.f;
   __device__ __forceinline__ void add(float x) {
     float y = x - c;
@@ -69,23 +99,27 @@ struct KSum {
     s = t;
   }
   __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+  __device__ __forceinline__ FF red() const { return FF{s, -c}; }
 };
 struct DSum {
+  using Red = double;
   double s = 0.0;
   __device__ __forceinline__ void add(double x) { s += x; }
   __device__ __forceinline__ double val() const { return s; }
+  __device__ __forceinline__ double red() const { return s; }
 };
 template <typename R> struct AccOf;
 template <> struct AccOf<float> { using type = KSum; };
 template <> struct AccOf<double> { using type = DSum; };
 
-// Deterministic grid reduction of NV doubles: block partials are written in
-// block order and the last block to arrive sums them in a fixed order, so two
-// identical launches give bit-identical totals.  Returns true in thread 0 of
-// the last block, with `total` filled; the counter is reset for the next
-// launch (graph replays reuse it).  All threads of every block must call it.
-template <int NV>
-__device__ __forceinline__ bool grid_reduce(double (&v)[NV], const RedBuf rb, double (&total)[NV]) {
+// Deterministic grid reduction of NV values (doubles, or float-float warp
+// inputs): block partials are written in block order and the last block to
+// arrive sums them in a fixed order, so two identical launches give
+// bit-identical totals.  Returns true in thread 0 of the last block, with
+// `total` filled; the counter is reset for the next launch (graph replays
+// reuse it).  All threads of every block must call it.
+template <int NV, typename T>
+__device__ __forceinline__ bool grid_reduce(const T (&v)[NV], const RedBuf rb, double (&total)[NV]) {
   __shared__ double sh[NV][32];
   __shared__ int am_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -140,8 +174,8 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], const RedBuf rb, do
 // Block sums of NV doubles written to out[blockIdx.x * NV + i] by thread 0:
 // the partials of a reduction that a later kernel completes in block order
 // (no fence or arrival counter in the pass).  All threads must call it.
-template <int NV>
-__device__ __forceinline__ void block_partials(const double (&v)[NV], double* out) {
+template <int NV, typename T>
+__device__ __forceinline__ void block_partials(const T (&v)[NV], double* out) {
   __shared__ double sh[NV][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll

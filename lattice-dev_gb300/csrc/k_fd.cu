@@ -241,7 +241,8 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   }
 
   if (MODE == 2) {
-    double v[2] = {acc_ge.val(), acc_pe.val()}, tot[2];
+    const typename Acc::Red v[2] = {acc_ge.red(), acc_pe.red()};
+    double tot[2];
     if (grid_reduce<2>(v, a.rb, tot)) {
       DevScalars* sc = a.sc;
       const double ac = sc->a;

@@ -382,29 +382,42 @@ __global__ void reduce_parts_kernel(const float* __restrict__ part, int nblk, in
 
 // ------------------------------------------------------------ pointwise
 // channels-last BF16 input [lat][site][8] from four FP32/FP64 channel arrays,
-// normalised: (x - shift) * scale; channels 4..7 are zero
+// normalised: (x u - shift) * scale = x (u scale) - shift scale in FP32 (the
+// result is rounded to BF16); channels 4..7 are zero.  The unit factors u
+// (a, 1/a) and the affine coefficients are formed once per block.
 template <typename R>
 __global__ void pack_kernel(PackArgs a) {
-  const int64_t total = a.nlat * a.N;
-  double u[4] = {1.0, 1.0, 1.0, 1.0};
-  if (a.sc) {
-    const double av = __ldcg(&a.sc->a);
-    u[0] = u[1] = av;
-    u[2] = u[3] = 1.0 / av;
-  }
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t l = i / a.N, s = i % a.N;
-    const int64_t base = a.idx ? (int64_t)a.idx[l] * a.lat_stride : l * a.lat_stride;
-    __align__(16) __nv_bfloat16 v[8];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const R* p = static_cast<const R*>(a.ch[c]);
-      const float x = (float)(((double)p[base + s] * u[c] - a.shift[c]) * a.scale[c]);
-      v[c] = __float2bfloat16_rn(x);
+  __shared__ float mul_sh[4], add_sh[4];
+  if (threadIdx.x == 0) {
+    double u[4] = {1.0, 1.0, 1.0, 1.0};
+    if (a.sc) {
+      const double av = __ldcg(&a.sc->a);
+      u[0] = u[1] = av;
+      u[2] = u[3] = 1.0 / av;
     }
+    for (int c = 0; c < 4; ++c) {
+      mul_sh[c] = (float)(u[c] * a.scale[c]);
+      add_sh[c] = (float)(-a.shift[c] * a.scale[c]);
+    }
+  }
+  __syncthreads();
+  float mul[4], add[4];
 #pragma unroll
-    for (int c = 4; c < 8; ++c) v[c] = __float2bfloat16_rn(0.f);
-    *reinterpret_cast<uint4*>(a.out + i * 8) = *reinterpret_cast<const uint4*>(v);
+  for (int c = 0; c < 4; ++c) mul[c] = mul_sh[c], add[c] = add_sh[c];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t l = 0; l < a.nlat; ++l) {
+    const int64_t base = a.idx ? (int64_t)a.idx[l] * a.lat_stride : l * a.lat_stride;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.N; s += stride) {
+      __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const R* p = static_cast<const R*>(a.ch[c]);
+        v[c] = __float2bfloat16_rn(fmaf((float)p[base + s], mul[c], add[c]));
+      }
+#pragma unroll
+      for (int c = 4; c < 8; ++c) v[c] = __float2bfloat16_rn(0.f);
+      *reinterpret_cast<uint4*>(a.out + (l * a.N + s) * 8) = *reinterpret_cast<const uint4*>(v);
+    }
   }
 }
 
@@ -477,10 +490,16 @@ __global__ void repack_kernel(const float* __restrict__ W, int ci, int co, __nv_
 // a^3 Delta_f = out[s][f] / tscale[f] (units 1); a = 1 in Minkowski
 template <typename R>
 __global__ void corr_kick_kernel(CorrArgs a) {
-  double av = 1.0;
-  if (a.conf) av = __ldcg(&a.sc->a);
-  const double f = a.units ? av : av * av * av * av;  // a^4 Delta = a (a^3 Delta)
-  const R c0 = (R)(a.hk * f / a.tscale[0]), c1 = (R)(a.hk * f / a.tscale[1]);
+  __shared__ double c_sh[2];  // the coefficients once per block (FP64 divisions)
+  if (threadIdx.x == 0) {
+    double av = 1.0;
+    if (a.conf) av = __ldcg(&a.sc->a);
+    const double f = a.units ? av : av * av * av * av;  // a^4 Delta = a (a^3 Delta)
+    c_sh[0] = a.hk * f / a.tscale[0];
+    c_sh[1] = a.hk * f / a.tscale[1];
+  }
+  __syncthreads();
+  const R c0 = (R)c_sh[0], c1 = (R)c_sh[1];
   R* p0 = static_cast<R*>(a.pi);
   R* p1 = p0 + a.N;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.N; s += (int64_t)gridDim.x * blockDim.x) {
@@ -557,8 +576,7 @@ int wgrad(const WgradArgs& a, int cx, int cd, int nblk, float* dW, float* db, cu
 }
 
 int pack(const PackArgs& a, int fp64, int nsm, cudaStream_t s) {
-  const int64_t total = a.nlat * a.N;
-  const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)nsm * 8);
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((a.N + 255) / 256, (int64_t)nsm * 8));
   if (fp64) pack_kernel<double><<<grid, 256, 0, s>>>(a);
   else pack_kernel<float><<<grid, 256, 0, s>>>(a);
   if (g_launch_counter) ++*g_launch_counter;

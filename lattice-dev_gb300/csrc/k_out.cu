@@ -311,9 +311,10 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
       }
     }
   }
-  double v[8], tot[8];
+  typename Acc::Red v[8];
+  double tot[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = s[i].val();
+  for (int i = 0; i < 8; ++i) v[i] = s[i].red();
   if (grid_reduce<8>(v, a.rb, tot)) {
     for (int i = 0; i < 8; ++i) {
       a.sc->red[i] = tot[i];
@@ -350,7 +351,8 @@ __global__ void __launch_bounds__(256) parseval_kernel(const C* F, int nx, int n
       acc.add(w * k2 * (v.x * v.x + v.y * v.y));
     }
   }
-  double vv[1] = {acc.val()}, t[1];
+  const typename Acc::Red vv[1] = {acc.red()};
+  double t[1];
   if (grid_reduce<1>(vv, rb, t)) sc->red[slot] = t[0];
 }
 

@@ -468,7 +468,8 @@ __global__ void __launch_bounds__(256) sep_kernel(SepArgs a) {
         lap_o[offB + pos * st] = vi[q];
       }
     }
-    double vals[5] = {ke.val(), pe.val(), ge.val(), mA.val(), mB.val()}, tot[5];
+    const typename Acc::Red vals[5] = {ke.red(), pe.red(), ge.red(), mA.red(), mB.red()};
+    double tot[5];
     if (grid_reduce<5>(vals, a.rb, tot)) {
       DevScalars* w = a.sc;
       if (a.conf) {
@@ -520,7 +521,8 @@ __global__ void __launch_bounds__(256) sep_kernel(SepArgs a) {
         }
       }
       if (a.conf) {
-        double vals[1] = {ge.val()}, tot[1];
+        const typename Acc::Red vals[1] = {ge.red()};
+        double tot[1];
         if (grid_reduce<1>(vals, a.rb, tot)) a.sc->gsum[1] = tot[0];
       }
     } else {
@@ -557,7 +559,8 @@ __global__ void __launch_bounds__(256) sep_kernel(SepArgs a) {
         }
       }
       if (a.conf) {
-        double vals[1] = {ge.val()}, tot[1];
+        const typename Acc::Red vals[1] = {ge.red()};
+        double tot[1];
         if (grid_reduce<1>(vals, a.rb, tot)) {
           DevScalars* w = a.sc;
           const double GE2 = (w->gsum[0] + w->gsum[1] + tot[0]) / (a1 * a1) / a.Nd;

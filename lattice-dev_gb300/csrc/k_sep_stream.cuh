@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   cp_wait_all();
   if (RUNS) return;
   // this block's sums; launch_sep_finalize completes them after pass Z
-  const double vals[4] = {pe.val(), ge.val(), mA.val(), mB.val()};
+  const FF vals[4] = {pe.red(), ge.red(), mA.red(), mB.red()};
   block_partials<4>(vals, a.rb.partials + SEP_PART_X);
 }
 
@@ -500,10 +500,10 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   cp_wait_all();
   if constexpr (!CONF) return;
   if constexpr (AXIS == 1) {
-    const double vals[1] = {ge.val()};
+    const FF vals[1] = {ge.red()};
     block_partials<1>(vals, a.rb.partials + SEP_PART_Y);
   } else {
-    const double vals[2] = {ge.val(), ke.val()};
+    const FF vals[2] = {ge.red(), ke.red()};
     block_partials<2>(vals, a.rb.partials + SEP_PART_Z);
   }
 }

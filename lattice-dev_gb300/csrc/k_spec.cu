@@ -15,6 +15,8 @@
 // after the kick and the drift coefficient h'/a^2 before it starts, and kick
 // and drift run as ONE sweep over HBM.  The drift's KE2 and the new PE are
 // reduced deterministically and the last block applies the ysclp update.
+#include <algorithm>
+
 #include "engine.hpp"
 
 namespace lat {
@@ -80,7 +82,14 @@ __device__ __forceinline__ Coef coefs(const PwArgs& a, bool conf) {
 
 template <typename R, bool KAHAN, int NF, bool CONF, int MODE, bool GWD>
 __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
-  const Coef co = coefs(a, CONF);
+  // the FP64 scalar chain once per block (its divisions would load the FP64
+  // pipe with every thread's copy), shared through shared memory
+  __shared__ Coef co_sh;
+  if (CONF) {
+    if (threadIdx.x == 0) co_sh = coefs(a, true);
+    __syncthreads();
+  }
+  const Coef co = CONF ? co_sh : coefs(a, false);
   const R ck = (R)co.ck, cv = (R)co.cv, cd = (R)co.cd;
   const int64_t N = a.N;
   R* phi = static_cast<R*>(a.phi);
@@ -175,7 +184,8 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
   }
 
   if (CONF) {
-    double v[3] = {acc_ke.val(), acc_pe.val(), acc_ge.val()}, tot[3];
+    const typename Acc::Red v[3] = {acc_ke.red(), acc_pe.red(), acc_ge.red()};
+    double tot[3];
     if (grid_reduce<3>(v, a.rb, tot)) {
       DevScalars* sc = a.sc;
       if (bad(tot[0]) || bad(tot[1]) || bad(tot[2])) sc->err |= 1u;
@@ -198,16 +208,24 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
   }
 }
 
+// grid-stride launches: at most one block per `block` work items, so a small
+// lattice does not launch (and reduce over) idle blocks
+inline int clamp_grid(int grid, int64_t items, int block) {
+  const int64_t need = (items + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(grid, need));
+}
+
 template <typename R, bool KAHAN, int NF, bool CONF>
 int pw_go(const PwArgs& a, cudaStream_t s) {
   const bool gw = a.u != nullptr;
+  const int grid = clamp_grid(a.grid, gw ? 6 * a.N : (a.N + 3) / 4, a.block);
   switch (a.mode) {
-    case PW_KD: pw_kernel<R, KAHAN, NF, CONF, PW_KD, false><<<a.grid, a.block, 0, s>>>(a); break;
+    case PW_KD: pw_kernel<R, KAHAN, NF, CONF, PW_KD, false><<<grid, a.block, 0, s>>>(a); break;
     case PW_DRIFT:
-      if (gw) pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, true><<<a.grid, a.block, 0, s>>>(a);
-      else pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, false><<<a.grid, a.block, 0, s>>>(a);
+      if (gw) pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, true><<<grid, a.block, 0, s>>>(a);
+      else pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, false><<<grid, a.block, 0, s>>>(a);
       break;
-    case PW_KICK: pw_kernel<R, KAHAN, NF, CONF, PW_KICK, false><<<a.grid, a.block, 0, s>>>(a); break;
+    case PW_KICK: pw_kernel<R, KAHAN, NF, CONF, PW_KICK, false><<<grid, a.block, 0, s>>>(a); break;
     default: return set_error(LAT_ERR_ARG, "bad pointwise mode");
   }
   if (g_launch_counter) ++*g_launch_counter;
@@ -251,7 +269,8 @@ __global__ void __launch_bounds__(256) kmul_kernel(KmulArgs a) {
     F[m] = v;
   }
   if (a.store_ge2) {
-    double v[1] = {acc.val()}, t[1];
+    const typename Acc::Red v[1] = {acc.red()};
+    double t[1];
     if (grid_reduce<1>(v, a.rb, t)) {
       a.sc->ge2 = t[0] * a.invN;
       if (bad(t[0])) a.sc->err |= 1u;
@@ -268,7 +287,8 @@ __global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars
     const float4 v = __ldcs(pi + i);
     s.add((v.x * v.x + v.y * v.y) + (v.z * v.z + v.w * v.w));
   }
-  double vals[1] = {s.val()}, tot[1];
+  const FF vals[1] = {s.red()};
+  double tot[1];
   if (grid_reduce<1>(vals, rb, tot)) {
     sc->ke_cur = tot[0];
     if (bad(tot[0])) sc->err |= 1u;
@@ -284,8 +304,9 @@ int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s) {
 }
 
 int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
-  if (precision == LAT_FP64) kmul_kernel<double, double2><<<a.grid, a.block, 0, s>>>(a);
-  else kmul_kernel<float, float2><<<a.grid, a.block, 0, s>>>(a);
+  const int grid = clamp_grid(a.grid, ((int64_t)a.nx / 2 + 1) * a.ny * a.nz * a.nf, a.block);
+  if (precision == LAT_FP64) kmul_kernel<double, double2><<<grid, a.block, 0, s>>>(a);
+  else kmul_kernel<float, float2><<<grid, a.block, 0, s>>>(a);
   if (g_launch_counter) ++*g_launch_counter;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "kmul launch");
