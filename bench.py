@@ -600,32 +600,32 @@ def run_fd_case(L, args, local):
     return 0
 
 
-CONV_FLOPS_PER_SITE = {  # tensor-core FLOPs per site as launched (padded channels) and useful
-    "conv1": (27 * 8 * 32 * 2, 27 * 4 * 32 * 2),
-    "conv2": (27 * 32 * 32 * 2, 27 * 32 * 32 * 2),
-    "conv3": (27 * 32 * 8 * 2, 27 * 32 * 2 * 2),
+CONV_FLOPS_PER_SITE = {  # algorithmic tensor FLOPs per site (real channels: 4 -> 32 -> 32 -> 2)
+    "conv1": 27 * 4 * 32 * 2,
+    "conv2": 27 * 32 * 32 * 2,
+    "conv3": 27 * 32 * 2 * 2,
 }
 
 
 def conv_roofline(L, net, n, reps=10):
     """Per-layer device time of the forward pass on an n^3 lattice and the
-    tensor FLOP rate against the measured dense BF16 peak."""
+    algorithmic tensor FLOP rate against the measured dense BF16 peak."""
     ms = net.time_forward((n, n, n), reps)
     pk, kind = peaks()
     peak = float(pk.get("bf16_tflops", 1900.0))
     N = n ** 3
     out = {"lattice": n, "pack_ms": ms[0]}
     for i, name in enumerate(("conv1", "conv2", "conv3")):
-        launched, useful = CONV_FLOPS_PER_SITE[name]
         t = ms[i + 1] * 1e-3
-        out[name] = {"ms": ms[i + 1], "tflops_launched": N * launched / t / 1e12,
-                     "tflops_useful": N * useful / t / 1e12}
+        out[name] = {"ms": ms[i + 1], "tflops": N * CONV_FLOPS_PER_SITE[name] / t / 1e12}
     tot = sum(ms[1:]) * 1e-3
-    ach = N * sum(v[0] for v in CONV_FLOPS_PER_SITE.values()) / tot / 1e12
+    ach = N * sum(CONV_FLOPS_PER_SITE.values()) / tot / 1e12
     out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                        "peak_kind": kind + " dense bf16 (cuBLAS burst)",
-                       "note": "conv1 (4 padded to 8 -> 32) and conv2 (32->32) on tcgen05.mma with TMEM "
-                               "accumulators when nx % 64 == 0, conv3 (32->2) on mma.sync; BF16 in, FP32 accumulate"}
+                       "note": "algorithmic FLOPs (the 4-channel input and the 2 outputs unpadded); conv1 "
+                               "(4 padded to 8 -> 32) and conv2 (32->32) on tcgen05.mma with TMEM accumulators "
+                               "when nx % 64 == 0, conv3 (32->2) weights-stationary on mma.sync; BF16 in, "
+                               "FP32 accumulate"}
     return out
 
 

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 
 #include "common.cuh"
 #include "gelu.cuh"
@@ -39,6 +40,9 @@ __device__ __forceinline__ void cp16(void* s, const void* g) {
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+template <int K> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
+}
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
@@ -251,6 +255,162 @@ __global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
       }
     }
   }
+}
+
+// ----------------------------------------------------- output layer, 32 -> 2
+// The direct form above re-reads 27 taps x 32 input channels of the halo
+// (1.7 KB per site) for only two output channels.  Here the weights stay in
+// the MMA's A fragments and the input sites are its N side: for a staged
+// input plane and tap row dz, D[(tap, co)][site'] = sum_ci W[tap][co][ci]
+// x[site'][ci] for the 9 (dy, dx) taps x 2 outputs (18 rows of two m16
+// tiles), over every staged site (the item's TYO output rows plus one halo
+// row on either side, whole x-rows of NXO sites, so the x halo is the row
+// itself).  D goes to shared memory; each thread then adds, for its output
+// site, the 9 D values of its neighbours in a fixed order.
+//
+// An item marches through zc output planes: input plane zA - 1 + j is staged
+// once (its successor's copies in flight meanwhile) and serves output planes
+// j (tap row 0), j - 1 (row 1) and j - 2 (row 2), which completes; three
+// rotating accumulators per thread hold the planes in progress.  D is
+// double-buffered when two blocks per SM still fit, so the sums of one tap
+// row overlap the MMAs of the next.  Input rows are 64 bytes, 16-byte chunks
+// swizzled by (site >> 1) & 3 so the 8 rows of an ldmatrix fall in distinct
+// banks.
+template <int NXO, int TYO>
+struct OutGeom {
+  static constexpr int HR = TYO + 2, NS = HR * NXO;    // staged rows and sites per plane
+  static constexpr int DS = NS + 8;                    // D row stride (floats): 64-bit stores conflict-free
+  static constexpr int XIN = NS * 64;                  // bytes per staged plane
+  static constexpr int DB = 18 * DS * 4;               // bytes per D buffer
+  static constexpr int NDB = 2 * XIN + 2 * DB <= 110 * 1024 ? 2 : 1;
+  static constexpr int SMEM = 2 * XIN + NDB * DB;
+  static_assert((NS / 8) % 8 == 0, "n-tiles divide evenly over 8 warps");
+  static_assert(TYO * NXO == 256, "one output site per thread");
+};
+
+__device__ __forceinline__ int swz(int site, int chunk) { return site * 64 + ((chunk ^ ((site >> 1) & 3)) << 4); }
+
+template <int NXO, int TYO>
+__global__ void __launch_bounds__(256) out_conv_kernel(ConvArgs a, int zc) {
+  using G = OutGeom<NXO, TYO>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  unsigned char* xin = smraw;                                   // [2][NS] x 64 bytes (swizzled)
+  float* dsm = reinterpret_cast<float*>(smraw + 2 * G::XIN);   // [NDB][18][DS]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t4 = lane & 3;
+  // A fragments: [dz][m tile][k step]; row R = 2 (3 dy + dx) + co of m tile R / 16, zero beyond 18
+  uint32_t af[3][2][2][4];
+#pragma unroll
+  for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int R = 16 * mt + g + ((r & 1) ? 8 : 0);
+          const int k = 16 * ks + 2 * t4 + ((r & 2) ? 8 : 0);
+          uint32_t v = 0;
+          if (R < 18) {
+            const int tap = dz * 9 + R / 2, co = R % 2;
+            v = *reinterpret_cast<const uint32_t*>(a.w + ((int64_t)tap * 8 + co) * 32 + k);
+          }
+          af[dz][mt][ks][r] = v;
+        }
+  const float b0 = a.bias ? a.bias[0] : 0.f, b1 = a.bias ? a.bias[1] : 0.f;
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  const int tiles_y = a.ny / TYO, zchunks = (a.nz + zc - 1) / zc;
+  const int64_t items_per = (int64_t)tiles_y * zchunks, nitems = items_per * a.nlat;
+  const int ox = tid % NXO, oy = tid / NXO;  // this thread's output site within the item
+
+  auto stage = [&](int buf, const __nv_bfloat16* src, int y0, int z) {
+    z = z < 0 ? z + a.nz : (z >= a.nz ? z - a.nz : z);
+    unsigned char* dst = xin + buf * G::XIN;
+    for (int i = tid; i < G::NS * 4; i += 256) {
+      const int site = i >> 2, c = i & 3;
+      const int hy = site / NXO, x = site % NXO;
+      int y = y0 - 1 + hy;
+      y = y < 0 ? y + a.ny : (y >= a.ny ? y - a.ny : y);
+      cp16(dst + swz(site, c), src + (((int64_t)z * a.ny + y) * NXO + x) * 32 + c * 8);
+    }
+    cp_commit();
+  };
+  // D of tap row DZ for every staged site of plane buffer xb into D buffer db
+  auto mma_row = [&](auto dzc, const unsigned char* xb, float* db) {
+    constexpr int DZ = decltype(dzc)::value;
+#pragma unroll 1
+    for (int nt = warp; nt < G::NS / 8; nt += 8) {
+      uint32_t b[4];
+      ldsm_x4(b, xb + swz(nt * 8 + (lane & 7), lane >> 3));
+      float d0[4] = {0.f, 0.f, 0.f, 0.f}, d1[4] = {0.f, 0.f, 0.f, 0.f};
+      mma16816(d0, af[DZ][0][0], b[0], b[1]);
+      mma16816(d0, af[DZ][0][1], b[2], b[3]);
+      mma16816(d1, af[DZ][1][0], b[0], b[1]);
+      mma16816(d1, af[DZ][1][1], b[2], b[3]);
+      const int col = nt * 8 + 2 * t4;
+      *reinterpret_cast<float2*>(db + g * G::DS + col) = make_float2(d0[0], d0[1]);
+      *reinterpret_cast<float2*>(db + (g + 8) * G::DS + col) = make_float2(d0[2], d0[3]);
+      if (g < 2) *reinterpret_cast<float2*>(db + (16 + g) * G::DS + col) = make_float2(d1[0], d1[1]);
+    }
+  };
+  // this thread's output site: the 9 (dy, dx) taps of D buffer db, in a fixed order
+  auto gather = [&](const float* db, float& c0, float& c1) {
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        int hx = ox + dx - 1;
+        hx = hx < 0 ? hx + NXO : (hx >= NXO ? hx - NXO : hx);
+        const int site = (oy + dy) * NXO + hx, R = 2 * (3 * dy + dx);
+        c0 += db[R * G::DS + site];
+        c1 += db[(R + 1) * G::DS + site];
+      }
+    }
+  };
+
+  int pb = 0;  // D buffer of the next MMA pass
+  for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int64_t li = item / items_per;
+    const int64_t rr = item % items_per;
+    const int y0 = (int)(rr % tiles_y) * TYO, zA = (int)(rr / tiles_y) * zc;
+    const int nzs = min(zc, a.nz - zA);
+    const __nv_bfloat16* src = a.in + li * Nsite * 32;
+    float* outp = a.outf + (li * Nsite + (int64_t)(y0 + oy) * NXO + ox) * 2;
+    // accumulators of output planes j (n), j - 1 (m), j - 2 (l) relative to zA
+    float n0 = 0.f, n1 = 0.f, m0 = 0.f, m1 = 0.f, l0 = 0.f, l1 = 0.f;
+    stage(0, src, y0, zA - 1);
+#pragma unroll 1
+    for (int j = 0; j <= nzs + 1; ++j) {
+      if (j <= nzs) {
+        stage((j + 1) & 1, src, y0, zA + j);
+        cp_async_wait<1>();
+      } else {
+        cp_wait_all();
+      }
+      __syncthreads();  // plane j landed; the previous plane's last sums are done
+      const unsigned char* xb = xin + (j & 1) * G::XIN;
+      float* dA = dsm + pb * (G::NDB - 1) * 18 * G::DS;         // D buffers of this plane's passes
+      float* dB = dsm + (pb ^ 1) * (G::NDB - 1) * 18 * G::DS;
+      const bool r0 = j < nzs, r1 = j >= 1 && j - 1 < nzs, r2 = j >= 2;  // output planes j, j-1, j-2 exist
+      // tap row 0 -> plane j, row 1 -> plane j - 1, row 2 -> plane j - 2 (uniform branches)
+      if (r0) mma_row(std::integral_constant<int, 0>{}, xb, dA);
+      __syncthreads();
+      if (r0) gather(dA, n0, n1);
+      if (G::NDB == 1) __syncthreads();
+      if (r1) mma_row(std::integral_constant<int, 1>{}, xb, dB);
+      __syncthreads();
+      if (r1) gather(dB, m0, m1);
+      if (G::NDB == 1) __syncthreads();
+      if (r2) mma_row(std::integral_constant<int, 2>{}, xb, dA);
+      __syncthreads();
+      if (r2) {
+        gather(dA, l0, l1);
+        *reinterpret_cast<float2*>(outp + (int64_t)(zA + j - 2) * a.ny * NXO * 2) = make_float2(l0 + b0, l1 + b1);
+      }
+      pb ^= 1;  // the next plane's first pass writes the buffer this plane's row 1 used
+      l0 = m0, l1 = m1, m0 = n0, m1 = n1, n0 = 0.f, n1 = 0.f;
+    }
+  }
+  cp_wait_all();
 }
 
 // ------------------------------------------------------- weight gradient
@@ -526,6 +686,33 @@ int conv_go(const ConvArgs& a, int nsm, cudaStream_t s) {
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "conv launch");
 }
 
+template <int NXO, int TYO>
+int out_conv_go(const ConvArgs& a, int nsm, cudaStream_t s) {
+  constexpr int smem = OutGeom<NXO, TYO>::SMEM;
+  auto k = out_conv_kernel<NXO, TYO>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "output conv smem attribute");
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+  if (per_sm < 1) per_sm = 1;
+  // output planes per item: the fewest rounds of items over the resident
+  // blocks, counting an item's two extra input planes
+  const int64_t slots = (int64_t)nsm * per_sm, items_xy = (int64_t)(a.ny / TYO) * a.nlat;
+  int zc = 16;
+  int64_t best = -1;
+  for (int c = 16; c >= 2; c /= 2) {
+    const int64_t items = items_xy * ((a.nz + c - 1) / c);
+    const int64_t cost = ((items + slots - 1) / slots) * (std::min(c, a.nz) + 2);
+    if (best < 0 || cost < best) best = cost, zc = c;
+  }
+  const int64_t nitems = items_xy * ((a.nz + zc - 1) / zc);
+  const int64_t grid = std::min<int64_t>(nitems, slots);
+  k<<<(unsigned)grid, 256, smem, s>>>(a, zc);
+  if (g_launch_counter) ++*g_launch_counter;
+  e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "output conv launch");
+}
+
 }  // namespace
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s) {
@@ -540,7 +727,12 @@ int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s) {
                                                         : conv_go<8, 32, EPI_GELU, false>(a, nsm, s);
   if (ca == 32 && cb == 32 && epi == EPI_GELU) return sz ? conv_go<32, 32, EPI_GELU, true>(a, nsm, s)
                                                          : conv_go<32, 32, EPI_GELU, false>(a, nsm, s);
-  if (ca == 32 && cb == 8 && epi == EPI_LINEAR) return conv_go<32, 8, EPI_LINEAR, false>(a, nsm, s);
+  if (ca == 32 && cb == 8 && epi == EPI_LINEAR) {
+    // whole x-rows of 64 or 128 sites: the weights-stationary kernel
+    if (a.nx == 64 && a.ny % 4 == 0) return out_conv_go<64, 4>(a, nsm, s);
+    if (a.nx == 128 && a.ny % 2 == 0) return out_conv_go<128, 2>(a, nsm, s);
+    return conv_go<32, 8, EPI_LINEAR, false>(a, nsm, s);
+  }
   if (ca == 8 && cb == 32 && epi == EPI_BWD) return conv_go<8, 32, EPI_BWD, false>(a, nsm, s);
   if (ca == 32 && cb == 32 && epi == EPI_BWD) return conv_go<32, 32, EPI_BWD, false>(a, nsm, s);
   return set_error(LAT_ERR_UNSUPPORTED, "conv shape");
