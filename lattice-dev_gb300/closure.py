@@ -220,9 +220,16 @@ def evaluate(s: Setup, net, seeds, t_eval, every=3, coarse_precision=L.FP32_KAHA
             if s.background == L.BG_CONFORMAL:
                 c.set_scale_factor(1.0, 0.0)
                 c.calc_metric()
-            for kk in (k1, kc - k1):
-                if kk:
-                    c.prepare_symp(s.order, dtc, kk)
+            # both segments' graphs built outside the timed region (the
+            # second with the network attached: the graph cache keys on it)
+            if k1:
+                c.prepare_symp(s.order, dtc, k1)
+            if kc - k1:
+                if attach:
+                    c.attach_closure(net, every, s.units)
+                c.prepare_symp(s.order, dtc, kc - k1)
+                if attach:
+                    c.attach_closure(None)
             c.sync()
             c.mark(0)
             if k1:

@@ -72,6 +72,8 @@ struct GraphEntry {
   int cur_after, ucur_after;
   void *fldc, *fldp;              // current compensation / momentum buffers at capture
   void *fldc_after, *fldp_after;  // and after the captured call
+  uint64_t cl_key;                 // attached closure network (0: none), its cadence and units
+  int cl_every, cl_units;
   int64_t kernels;
   cudaGraphExec_t exec;
 };
@@ -529,6 +531,7 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
 // fields before the first of every cl_every kicks, and its force correction
 // applied after each kick (the kick itself is unchanged).
 int exec_closure(lat_s* h, const std::vector<Op>& ops) {
+  net::out_scale(h->cl_net, h->cl_tscale);  // the network's current normalisation
   int kicks = 0;
   for (const Op& o : ops) {
     switch (o.t) {
@@ -797,6 +800,10 @@ int symp_graph(lat_s* h, int32_t order, double dt, int32_t nsteps, bool run) {
   Emitter em = emitter(h, &ops, tg);
   RET(em.symp(order, dt, nsteps));
   const bool graphs = h->use_graphs && !h->timing;
+  // a graph holds the closure's buffers and its normalisation by value: it
+  // matches only the same network, normalisation, cadence and units
+  const uint64_t cl_key = h->cl_net ? net::net_key(h->cl_net) : 0;
+  const int cl_every = h->cl_net ? h->cl_every : 0, cl_units = h->cl_net ? h->cl_units : 0;
   if (!graphs) {
     if (!run) return LAT_OK;
     RET(exec_fused(h, ops));
@@ -805,7 +812,8 @@ int symp_graph(lat_s* h, int32_t order, double dt, int32_t nsteps, bool run) {
   }
   for (auto& ge : h->graphs) {
     if (ge.order == order && ge.dt == dt && ge.nsteps == nsteps && ge.cur == h->cur && ge.ucur == h->ucur &&
-        ge.fldc == h->fldc && ge.fldp == h->fldp) {
+        ge.fldc == h->fldc && ge.fldp == h->fldp && ge.cl_key == cl_key && ge.cl_every == cl_every &&
+        ge.cl_units == cl_units) {
       if (!run) return LAT_OK;
       CK(cudaGraphLaunch(ge.exec, h->stream));
       h->launches += ge.kernels;
@@ -819,6 +827,7 @@ int symp_graph(lat_s* h, int32_t order, double dt, int32_t nsteps, bool run) {
   }
   GraphEntry ge{};
   ge.order = order; ge.dt = dt; ge.nsteps = nsteps; ge.cur = h->cur; ge.ucur = h->ucur;
+  ge.cl_key = cl_key; ge.cl_every = cl_every; ge.cl_units = cl_units;
   ge.fldc = h->fldc; ge.fldp = h->fldp;
   void* const c_alt0 = h->fldc_alt;
   void* const p_alt0 = h->fldp_alt;
@@ -1835,7 +1844,7 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   CK(cudaStreamSynchronize(h->stream));
-  free_graphs(h);
+  // cached graphs stay: their key holds the closure state they were captured with
   if (!net) {
     if (h->cl_net) net::net_attach_ref(h->cl_net, -1);
     h->cl_net = nullptr;

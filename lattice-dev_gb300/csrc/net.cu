@@ -6,6 +6,7 @@
 // fields and momenta (phi, chi, pi_phi, pi_chi) at a kick to a correction of
 // the two forces: the kick uses V'(phi) - Delta, with Delta trained on
 // V'(F phi) - F V'(phi) of sharp-k filtered fine-lattice runs (lat_coarsen).
+#include <atomic>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -48,9 +49,12 @@ struct lat_net_s {
   int64_t launches = 0;
   int* err = nullptr;  // device error word of the tensor-memory convolutions (bounded waits)
   int attached = 0;    // lattices this network is attached to (lat_closure_attach)
+  uint64_t key = 0;    // unique per network and normalisation (kernel arguments captured in graphs)
 };
 
 namespace {
+
+std::atomic<uint64_t> g_net_keys{0};
 
 struct Guard {
   explicit Guard(lat_net_s* n) {
@@ -260,6 +264,8 @@ int* net_err(const lat_net_s* n) { return n->err; }
 
 void net_attach_ref(lat_net_s* n, int delta) { n->attached += delta; }
 
+uint64_t net_key(const lat_net_s* n) { return n->key; }
+
 }  // namespace net
 }  // namespace lat
 
@@ -272,6 +278,7 @@ int lat_net_create(lat_net_t** out, int32_t device, uint64_t seed) {
   *out = nullptr;
   lat_net_s* n = new lat_net_s();
   n->dev = device;
+  n->key = ++g_net_keys;
   Guard g(n);
   auto bail = [&](int st) {
     lat_net_destroy(n);
@@ -371,6 +378,7 @@ int lat_net_set_norm(lat_net_t* n, const double in_shift[4], const double in_sca
   if (out_scale[0] == 0.0 || out_scale[1] == 0.0) return set_error(LAT_ERR_ARG, "zero output scale");
   n->tscale[0] = out_scale[0];
   n->tscale[1] = out_scale[1];
+  n->key = ++g_net_keys;  // graphs captured with the old normalisation no longer match
   return LAT_OK;
 }
 

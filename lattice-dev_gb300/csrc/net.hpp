@@ -84,10 +84,11 @@ void out_scale(const lat_net_s* n, double out[2]);
 int net_device(const lat_net_s* n);
 int* net_err(const lat_net_s* n);
 void net_attach_ref(lat_net_s* n, int delta);
+uint64_t net_key(const lat_net_s* n);  // changes with every network and every normalisation
 
 int conv(const ConvArgs& a, int ca, int cb, int epi, int nsm, cudaStream_t s);
 // layers with 32 output channels on tcgen05 (k_conv_tc.cu): 32 -> 32 (forward and
-// backward data) and the 8-channel (4 padded) input layer; nx % 128 == 0, ny % 2 == 0
+// backward data) and the 8-channel (4 padded) input layer; nx % 64 == 0 (rows of 128 or 64 sites)
 bool conv_tc_ok(int ca, int cb, int epi, int nx, int ny);
 int conv_tc(const ConvArgs& a, int ca, int epi, int nsm, int* err, cudaStream_t s);
 int wgrad_blocks(int nsm);

@@ -245,3 +245,43 @@ def test_attached_network_cannot_be_destroyed(engine):
     g.attach_closure(None)
     net.close()  # detached: freed
     g.close()
+
+
+def test_closure_graphs_keyed_on_network_state(engine):
+    """Graphs of lat_symp are cached per closure state: a graph prepared with
+    the network attached is replayed after a detach and re-attach, and a new
+    normalisation (captured by value in the graph) is never replayed stale."""
+    c = L.make_config((32, 16, 16), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, precision=L.FP64,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    f, p = random_state((2, 16, 16, 32), seed=13, mean=0.5, amp=0.2)
+    net = engine.Net(seed=5)
+    q = np.random.default_rng(1).standard_normal(net.nparams).astype(np.float32) * 0.05
+    net.set_params(q)
+    norm_a = ([0.5, 0.0, 0.0, 0.0], [1.0, 1.0, 1.0, 1.0], [2.0, 3.0])
+    norm_b = ([0.5, 0.0, 0.0, 0.0], [1.0, 1.0, 1.0, 1.0], [0.5, 0.25])
+
+    def run(prepare, norm):
+        g = engine.Lattice(c)
+        g.set_state(f, p)
+        net.set_norm(*norm_a)
+        if prepare:  # graph built with the closure attached, then detached
+            g.attach_closure(net, 2, L.UNITS_PROGRAM)
+            g.prepare_symp(2, 0.02, 6)
+            g.attach_closure(None)
+        net.set_norm(*norm)
+        g.attach_closure(net, 2, L.UNITS_PROGRAM)
+        l0 = g.launch_count()
+        g.symp(2, 0.02, 6)
+        out = g.get_state(), g.launch_count() - l0
+        g.attach_closure(None)
+        g.close()
+        return out
+
+    fresh_a, _ = run(False, norm_a)
+    fresh_b, _ = run(False, norm_b)
+    assert not np.array_equal(fresh_a[1], fresh_b[1])  # the normalisation matters
+    replay_a, _ = run(True, norm_a)
+    assert np.array_equal(replay_a[0], fresh_a[0]) and np.array_equal(replay_a[1], fresh_a[1])
+    renorm, _ = run(True, norm_b)  # prepared under norm_a: must not be replayed
+    assert np.array_equal(renorm[0], fresh_b[0]) and np.array_equal(renorm[1], fresh_b[1])
+    net.close()
