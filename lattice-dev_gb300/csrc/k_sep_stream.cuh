@@ -29,9 +29,10 @@
 // cp.async at once, and runs the line transforms in a separate scratch, so the
 // next tile's HBM reads are in flight during the transforms.  Pass X: 128
 // threads per block; every warp stages and transforms its own lines with warp
-// barriers only.  Passes Y, Z: 16 (256-point lines) or 32 x-columns per
-// block, with a second slot for the momenta, which are needed only after the
-// transform.  Every update of a tile is written by the block that read it,
+// barriers only.  Passes Y, Z: 32 x-columns per block (128-byte rows of
+// momenta: at 16 columns the strided 64-byte rows ran both passes 4-6%
+// slower), with a second slot for the momenta, which are needed only after
+// the transform.  Every update of a tile is written by the block that read it,
 // so the passes also run in place.
 #pragma once
 #include "k_sep.cuh"
@@ -134,7 +135,7 @@ __device__ __forceinline__ void build_tables(const float2* twN, float dk2, float
 template <int AXIS, int N>
 struct STile {
   static constexpr int P = Split<N>::P, Q = Split<N>::Q;
-  static constexpr int LINES_YZ = N == 256 ? 16 : 32;  // x-columns of a Y, Z tile (64 or 128 bytes)
+  static constexpr int LINES_YZ = 32;  // x-columns of a Y, Z tile (128-byte rows of momenta)
   static constexpr int THREADS = AXIS == 0 ? 128 : P * LINES_YZ, LINES = THREADS / P;
   // X: one staged row per line (padded by P floats so the 32/P lines of a
   // warp start in different banks); Y, Z: one row of LINES x-columns per
