@@ -170,14 +170,22 @@ struct STile {
 // line A's first site.  Two fields: one pair (pair_lines = nlines).
 template <int AXIS>
 __device__ __forceinline__ int64_t tile_base(const SepArgs& a, int64_t l0, int64_t& pair) {
+  // 32-bit index arithmetic (the dispatch checks nlines < 2^31): 64-bit
+  // divisions by the runtime extents cost more than a tile's addressing
+  const uint32_t l = (uint32_t)l0;
+  uint32_t p = 0, r = l;
+  if (a.runs) {
+    const uint32_t pl = (uint32_t)a.pair_lines;
+    p = l / pl;
+    r = l - p * pl;
+  }
+  pair = p;
   const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
-  pair = l0 / a.pair_lines;
-  const int64_t r = l0 % a.pair_lines;
-  const int64_t pbase = pair * 2 * Ns;
-  if constexpr (AXIS == 0) return pbase + r * a.nx;
-  const int64_t plane = (int64_t)a.nx * a.ny;
-  const int64_t x0 = r % a.nx, o = r / a.nx;
-  return pbase + (AXIS == 1 ? o * plane : o * a.nx) + x0;
+  const int64_t pbase = (int64_t)p * 2 * Ns;
+  if constexpr (AXIS == 0) return pbase + (int64_t)r * a.nx;
+  const uint32_t nx = (uint32_t)a.nx;
+  const uint32_t o = r / nx, x0 = r - o * nx;
+  return pbase + (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0;
 }
 
 // Passes Y, Z: copy the early inputs (part 0: zs, both lines interleaved as
@@ -532,7 +540,8 @@ int stream_lines(int axis) {
 template <int N, bool RUNS>
 int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
   const int lines = stream_lines<N>(axis);
-  if (a.pair_lines <= 0 || a.nlines <= 0 || a.nlines % a.pair_lines || a.pair_lines % lines ||
+  if (a.pair_lines <= 0 || a.nlines <= 0 || a.nlines >= (int64_t{1} << 31) || a.nlines % a.pair_lines ||
+      a.pair_lines % lines ||
       (axis != 0 && a.nx % lines) || (!RUNS && (a.nf != 2 || a.nlines != a.pair_lines)) ||
       (RUNS && (a.conf || !a.shift_a || !a.shift_b)))
     return set_error(LAT_ERR_STATE, "streamed separable pass: lines do not form whole tiles");
