@@ -363,15 +363,23 @@ int exec_grav(lat_s* h, double hg) {
   return launch_grav(h->sc, hg, h->stream);
 }
 
-int exec_kd(lat_s* h, double hk, double hg, double hd) {
+// corr: the attached closure's force enters the kick (spectral lattices)
+int exec_kd(lat_s* h, double hk, double hg, double hd, bool corr = false) {
   if (spectral(h)) {
     RET(spectral_lap(h, conformal(h)));
     Timed t(h, LAT_K_KICKDRIFT);
     PwArgs a = pw_base(h);
     a.mode = PW_KD;
     a.hk = hk; a.hg = hg; a.hd = hd;
+    if (corr) {
+      a.corr = h->cl_b.out;
+      a.corr_ts[0] = h->cl_tscale[0];
+      a.corr_ts[1] = h->cl_tscale[1];
+      a.corr_units = h->cl_units;
+    }
     return launch_pointwise(a, h->prec, h->stream);
   }
+  if (corr) return set_error(LAT_ERR_STATE, "fused closure kick on a finite-difference lattice");
   // FD Minkowski: stencil kick + drift into the other buffer
   Timed t(h, LAT_K_KICKDRIFT);
   FdArgs a = fd_base(h);
@@ -527,25 +535,51 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
   return LAT_OK;
 }
 
-// Op list with the closure: plain passes, the network evaluated on the
-// fields before the first of every cl_every kicks, and its force correction
-// applied after each kick (the kick itself is unchanged).
+// Op list with the closure: the network evaluated on the fields before the
+// first of every cl_every kicks, and its force correction added after each
+// kick (the kick itself is unchanged).  On a spectral lattice the groups of
+// exec_fused (K D... in Minkowski, G K G D in conformal) run as the fused
+// kick+drift with the correction inside, the network evaluated before the
+// group with the scale factor after its first gravity half-step; every other
+// op runs on its own, a kick followed by the separate correction kernel.
 int exec_closure(lat_s* h, const std::vector<Op>& ops) {
   net::out_scale(h->cl_net, h->cl_tscale);  // the network's current normalisation
+  const bool conf = conformal(h);
+  const bool fuse = spectral(h) && !(conf && h->cfg.split_order == LAT_SPLIT_DEFROST);
+  const int fp64 = h->prec == LAT_FP64 ? 1 : 0;
   int kicks = 0;
-  for (const Op& o : ops) {
+  auto infer = [&](double hg) -> int {  // before the kick with index `kicks`
+    if (kicks++ % h->cl_every) return LAT_OK;
+    Timed t(h, LAT_K_OTHER);
+    const size_t fb = (size_t)h->N * h->rsz;
+    const void* ch[4] = {h->fld[h->cur], (const char*)h->fld[h->cur] + fb, h->fldp, (const char*)h->fldp + fb};
+    return net::infer(h->cl_net, ch, fp64, h->nx, h->ny, h->nz, h->cl_units ? h->sc : nullptr, hg, h->cl_b,
+                      h->stream);
+  };
+  size_t i = 0;
+  while (i < ops.size()) {
+    if (fuse && !conf && ops[i].t == 'K' && i + 1 < ops.size() && ops[i + 1].t == 'D') {
+      double hd = 0;
+      size_t j = i + 1;
+      while (j < ops.size() && ops[j].t == 'D') hd += ops[j++].h;
+      RET(infer(0.0));
+      RET(exec_kd(h, ops[i].h, 0.0, hd, true));
+      i = j;
+      continue;
+    }
+    if (fuse && conf && ops[i].t == 'G' && i + 3 < ops.size() && ops[i + 1].t == 'K' && ops[i + 2].t == 'G' &&
+        ops[i + 3].t == 'D' && ops[i].h == ops[i + 2].h) {
+      RET(infer(ops[i].h));
+      RET(exec_kd(h, ops[i + 1].h, ops[i].h, ops[i + 3].h, true));
+      i += 4;
+      continue;
+    }
+    const Op& o = ops[i++];
     switch (o.t) {
       case 'D': RET(exec_drift(h, o.h)); break;
       case 'G': RET(exec_grav(h, o.h)); break;
       case 'K': {
-        if (kicks % h->cl_every == 0) {
-          Timed t(h, LAT_K_OTHER);
-          const size_t fb = (size_t)h->N * h->rsz;
-          const void* ch[4] = {h->fld[h->cur], (const char*)h->fld[h->cur] + fb, h->fldp, (const char*)h->fldp + fb};
-          RET(net::infer(h->cl_net, ch, h->prec == LAT_FP64 ? 1 : 0, h->nx, h->ny, h->nz,
-                         h->cl_units ? h->sc : nullptr, h->cl_b, h->stream));
-        }
-        ++kicks;
+        RET(infer(0.0));
         RET(exec_kick(h, o.h));
         Timed t(h, LAT_K_OTHER);
         net::CorrArgs c{};
@@ -554,11 +588,11 @@ int exec_closure(lat_s* h, const std::vector<Op>& ops) {
         c.tscale[0] = h->cl_tscale[0];
         c.tscale[1] = h->cl_tscale[1];
         c.hk = o.h;
-        c.conf = conformal(h) ? 1 : 0;
+        c.conf = conf ? 1 : 0;
         c.units = h->cl_units;
         c.sc = h->sc;
         c.N = h->N;
-        RET(net::corr_kick(c, h->prec == LAT_FP64 ? 1 : 0, h->nsm, h->stream));
+        RET(net::corr_kick(c, fp64, h->nsm, h->stream));
         break;
       }
       default: break;

@@ -62,6 +62,12 @@ struct PwArgs {
   DevScalars* sc;
   RedBuf rb;
   int grid, block;
+  // learned-closure force of the kick (fused kick+drift with two fields):
+  // pi_f += hk (a^4 or a) corr[s][f] / corr_ts[f], a after the first
+  // gravity half-step; null: none
+  const float* corr;
+  double corr_ts[2];
+  int corr_units;  // 0: a^4 (program units), 1: a (conformal units)
 };
 int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s);
 

@@ -551,7 +551,9 @@ __global__ void pack_kernel(PackArgs a) {
   if (threadIdx.x == 0) {
     double u[4] = {1.0, 1.0, 1.0, 1.0};
     if (a.sc) {
-      const double av = __ldcg(&a.sc->a);
+      // the scale factor the kick sees: after a pending gravity half-step
+      // (the same expression as the gravity kernel's)
+      const double av = a.hg != 0.0 ? __ldcg(&a.sc->a) - a.hg * __ldcg(&a.sc->ap) / 6.0 : __ldcg(&a.sc->a);
       u[0] = u[1] = av;
       u[2] = u[3] = 1.0 / av;
     }

@@ -50,6 +50,7 @@ template <> struct Vec4<double> {
 struct Coef {
   double a0, ap0, a1, ap1, a2;
   double ck, cv, cd;
+  double cc[2];  // closure force coefficients (fused kick+drift with a correction)
 };
 
 // Scalar chain of one pass, identical in every block.
@@ -80,17 +81,32 @@ __device__ __forceinline__ Coef coefs(const PwArgs& a, bool conf) {
   return c;
 }
 
-template <typename R, bool KAHAN, int NF, bool CONF, int MODE, bool GWD>
+// CORR (fused kick+drift of two fields only): the kick adds the learned
+// closure's force hk (a1^4 or a1) corr[s][f] / corr_ts[f] after its own
+// update and before the drift, as the separate closure kick would
+template <typename R, bool KAHAN, int NF, bool CONF, int MODE, bool GWD, bool CORR = false>
 __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
+  static_assert(!CORR || (MODE == PW_KD && NF == 2), "the closure force enters the fused kick of two fields");
   // the FP64 scalar chain once per block (its divisions would load the FP64
   // pipe with every thread's copy), shared through shared memory
   __shared__ Coef co_sh;
-  if (CONF) {
-    if (threadIdx.x == 0) co_sh = coefs(a, true);
+  if (CONF || CORR) {
+    if (threadIdx.x == 0) {
+      Coef c = coefs(a, CONF);
+      if (CORR) {
+        const double av = CONF ? c.a1 : 1.0;  // a = 1 in Minkowski
+        const double f = a.corr_units ? av : av * av * av * av;
+        c.cc[0] = a.hk * f / a.corr_ts[0];
+        c.cc[1] = a.hk * f / a.corr_ts[1];
+      }
+      co_sh = c;
+    }
     __syncthreads();
   }
-  const Coef co = CONF ? co_sh : coefs(a, false);
+  const Coef co = (CONF || CORR) ? co_sh : coefs(a, false);
   const R ck = (R)co.ck, cv = (R)co.cv, cd = (R)co.cd;
+  const R cc[2] = {(R)co.cc[0], (R)co.cc[1]};
+  const float* __restrict__ corr = a.corr;
   const int64_t N = a.N;
   R* phi = static_cast<R*>(a.phi);
   R* phic = static_cast<R*>(a.phic);
@@ -99,7 +115,7 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
   using Acc = typename AccOf<R>::type;
   Acc acc_ke, acc_pe, acc_ge;
 
-  auto site = [&](R (&f)[NF], R (&c)[NF], R (&p)[NF], const R (&lp)[NF]) {
+  auto site = [&](R (&f)[NF], R (&c)[NF], R (&p)[NF], const R (&lp)[NF], const R (&dl)[NF]) {
     if (MODE == PW_KD || MODE == PW_KICK) {
       R dv[NF];
       model_dv<R, NF>(a.model, f, dv);
@@ -107,6 +123,7 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
       for (int l = 0; l < NF; ++l) {
         if (CONF && MODE == PW_KICK) acc_ge.add(-f[l] * lp[l]);
         p[l] = p[l] + (ck * lp[l] - cv * dv[l]);
+        if (CORR) p[l] += cc[l] * dl[l];
       }
       if (CONF && MODE == PW_KICK) acc_pe.add(model_v<R, NF>(a.model, f));
     }
@@ -133,17 +150,28 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
       P[l].load(pi + l * N + s0);
       if (MODE != PW_DRIFT) L[l].load(lap + l * N + s0);
     }
+    float4 D[2];  // closure force of the 4 sites, [site][field]
+    if (CORR) {
+      D[0] = __ldcs(reinterpret_cast<const float4*>(corr + 2 * s0));
+      D[1] = __ldcs(reinterpret_cast<const float4*>(corr + 2 * s0) + 1);
+    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      R f[NF], c[NF], p[NF], lp[NF];
+      R f[NF], c[NF], p[NF], lp[NF], dl[NF];
 #pragma unroll
       for (int l = 0; l < NF; ++l) {
         f[l] = F[l].v[j];
         c[l] = (KAHAN && MODE != PW_KICK) ? C[l].v[j] : R(0);
         p[l] = P[l].v[j];
         lp[l] = MODE != PW_DRIFT ? L[l].v[j] : R(0);
+        dl[l] = R(0);
       }
-      site(f, c, p, lp);
+      if (CORR) {
+        const float4 d = D[j / 2];
+        dl[0] = (R)((j & 1) ? d.z : d.x);
+        dl[NF - 1] = (R)((j & 1) ? d.w : d.y);
+      }
+      site(f, c, p, lp, dl);
 #pragma unroll
       for (int l = 0; l < NF; ++l) {
         F[l].v[j] = f[l];
@@ -160,15 +188,16 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
   }
   // tail (N not a multiple of 4)
   for (int64_t s = nvec * 4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
-    R f[NF], c[NF], p[NF], lp[NF];
+    R f[NF], c[NF], p[NF], lp[NF], dl[NF];
 #pragma unroll
     for (int l = 0; l < NF; ++l) {
       f[l] = phi[l * N + s];
       c[l] = (KAHAN && MODE != PW_KICK) ? phic[l * N + s] : R(0);
       p[l] = pi[l * N + s];
       lp[l] = MODE != PW_DRIFT ? lap[l * N + s] : R(0);
+      dl[l] = CORR ? (R)corr[2 * s + l] : R(0);
     }
-    site(f, c, p, lp);
+    site(f, c, p, lp, dl);
 #pragma unroll
     for (int l = 0; l < NF; ++l) {
       if (MODE != PW_KICK) phi[l * N + s] = f[l];
@@ -220,7 +249,17 @@ int pw_go(const PwArgs& a, cudaStream_t s) {
   const bool gw = a.u != nullptr;
   const int grid = clamp_grid(a.grid, gw ? 6 * a.N : (a.N + 3) / 4, a.block);
   switch (a.mode) {
-    case PW_KD: pw_kernel<R, KAHAN, NF, CONF, PW_KD, false><<<grid, a.block, 0, s>>>(a); break;
+    case PW_KD:
+      if constexpr (NF == 2) {
+        if (a.corr) {
+          pw_kernel<R, KAHAN, NF, CONF, PW_KD, false, true><<<grid, a.block, 0, s>>>(a);
+          break;
+        }
+      } else {
+        if (a.corr) return set_error(LAT_ERR_UNSUPPORTED, "the closure force needs two fields");
+      }
+      pw_kernel<R, KAHAN, NF, CONF, PW_KD, false><<<grid, a.block, 0, s>>>(a);
+      break;
     case PW_DRIFT:
       if (gw) pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, true><<<grid, a.block, 0, s>>>(a);
       else pw_kernel<R, KAHAN, NF, CONF, PW_DRIFT, false><<<grid, a.block, 0, s>>>(a);

@@ -236,9 +236,10 @@ namespace lat {
 namespace net {
 
 int infer(lat_net_s* n, const void* const ch[4], int fp64, int nx, int ny, int nz, const DevScalars* conformal_sc,
-          const InferBufs& b, cudaStream_t s) {
+          double hg, const InferBufs& b, cudaStream_t s) {
   PackArgs p{};
   p.sc = conformal_sc;
+  p.hg = hg;
   for (int c = 0; c < 4; ++c) {
     p.ch[c] = ch[c];
     p.shift[c] = n->shift[c];

@@ -46,6 +46,7 @@ struct PackArgs {
   int64_t lat_stride, nlat, N;
   double shift[4], scale[4];
   const DevScalars* sc;  // conformal units: fields times a, momenta over a (a from the scalar block)
+  double hg;             // a gravity half-step still to apply: a - hg ysclp / 6
   __nv_bfloat16* out;    // [nlat][N][8]
 };
 
@@ -78,8 +79,9 @@ struct InferBufs {
 };
 
 // forward pass of one lattice from four channel arrays (phi, chi, pi_phi, pi_chi)
+// (conformal units: hg is a gravity half-step the scale factor has still to take)
 int infer(lat_net_s* n, const void* const ch[4], int fp64, int nx, int ny, int nz, const DevScalars* conformal_sc,
-          const InferBufs& b, cudaStream_t s);
+          double hg, const InferBufs& b, cudaStream_t s);
 void out_scale(const lat_net_s* n, double out[2]);
 int net_device(const lat_net_s* n);
 int* net_err(const lat_net_s* n);
