@@ -39,6 +39,7 @@ struct FdArgs {
   DevScalars* sc;
   RedBuf rb;
   int ty, zc;          // tile: 32 x ty threads, zc planes per block
+  int vec;             // set by the launcher: 16-byte staging of the tile rows (FP32, nx % 32 == 0)
 };
 int launch_fd(const FdArgs& a, int precision, cudaStream_t s, int* nblocks_out);
 int fd_max_blocks(int nx, int ny, int nz, int ty, int zc);

@@ -14,6 +14,10 @@
 //       RANK3 = s2(z-1) + s2(z+1).
 // Each plane is staged once in shared memory (9 reads per site) and the
 // (c,s1,s2) of planes z-1, z, z+1 live in registers while the tile marches in z.
+// FP32 lattices whose rows are whole tiles stage the 32 interior values of a
+// row with 16-byte copies into rows of 40 (interior at column 4, halo at 3
+// and 36) and the two halo values with 4-byte copies; otherwise every value
+// is a 4-byte copy into rows of 34.
 #include "engine.hpp"
 
 namespace lat {
@@ -30,6 +34,10 @@ __device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem, int 
   if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
   else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int G> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(G) : "memory");
@@ -42,7 +50,8 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   constexpr int NC = NF + (GW ? 6 : 0);
   constexpr int TX = 32;
   const int TY = blockDim.y;
-  const int Wd = TX + 2, PL = Wd * (TY + 2);
+  const bool vec = a.vec != 0;
+  const int Wd = vec ? 40 : TX + 2, XO = vec ? 4 : 1, PL = Wd * (TY + 2);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);  // [3][NC][PL]: ring of planes z-1, z, z+1 (and the one in flight)
 
@@ -64,20 +73,51 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   // the same for every plane, so the wrap arithmetic runs once per block
   int slot_off[kFdMaxSlots];
   int nslot = 0;
+  // 16-byte staging: thread tid copies interior chunk tid (8 per row) or, after
+  // those, one halo value (2 per row); v_kind 1 / 2 / 0 (none)
+  int v_kind = 0, v_dst = 0, v_src = 0;
+  if (vec) {
+    const int nch = 8 * (TY + 2);
+    if (tid < nch) {
+      const int r = tid >> 3, ch = tid & 7;
+      v_kind = 1;
+      v_dst = r * Wd + 4 + 4 * ch;
+      v_src = pmod(y0 + r - 1, ny) * nx + x0 + 4 * ch;
+    } else if (tid < nch + 2 * (TY + 2)) {
+      const int h = tid - nch, r = h >> 1, side = h & 1;
+      v_kind = 2;
+      v_dst = r * Wd + (side ? 36 : 3);
+      v_src = pmod(y0 + r - 1, ny) * nx + pmod(side ? x0 + TX : x0 - 1, nx);
+    }
+  } else {
 #pragma unroll
-  for (int k = 0; k < kFdMaxSlots; ++k) {
-    const int i = tid + k * nthr;
-    slot_off[k] = 0;
-    if (i < PL) {
-      const int r = i / Wd, cc = i - r * Wd;
-      const int gx = pmod(x0 + cc - 1, nx), gy = pmod(y0 + r - 1, ny);
-      slot_off[k] = gy * nx + gx;
-      nslot = k + 1;
+    for (int k = 0; k < kFdMaxSlots; ++k) {
+      const int i = tid + k * nthr;
+      slot_off[k] = 0;
+      if (i < PL) {
+        const int r = i / Wd, cc = i - r * Wd;
+        const int gx = pmod(x0 + cc - 1, nx), gy = pmod(y0 + r - 1, ny);
+        slot_off[k] = gy * nx + gx;
+        nslot = k + 1;
+      }
     }
   }
   // issue the asynchronous copy of plane z into ring buffer b
   auto load_plane = [&](int z, int b) {
     const int64_t zo = (int64_t)pmod(z, nz) * plane;
+    if (vec) {
+      if (v_kind) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const R* src = (c < NF ? phi + (int64_t)c * N : uin + (int64_t)(c - NF) * N) + zo + v_src;
+          R* dst = sm + (b * NC + c) * PL + v_dst;
+          if (v_kind == 1) cp_async16(dst, src);
+          else cp_async_elem(dst, src, (int)sizeof(R));
+        }
+      }
+      cp_async_commit();
+      return;
+    }
 #pragma unroll
     for (int k = 0; k < kFdMaxSlots; ++k) {
       if (k < nslot) {
@@ -94,7 +134,7 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
 
   R wc[NC][3], ws1[NC][3], ws2[NC][3];
   R gxw[NF][2], gyw[NF][2];  // in-plane phi differences of planes z (slot 0) and z+1 (slot 1)
-  const int ctr = (ty + 1) * Wd + (tx + 1);
+  const int ctr = (ty + 1) * Wd + (tx + XO);
 
   auto fill = [&](int b, int slot) {
 #pragma unroll
@@ -256,12 +296,16 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
 }
 
 template <typename R, bool KAHAN, int NF, bool GW, bool SEVEN, int MODE>
-int go(const FdArgs& a, cudaStream_t s, int* nb) {
+int go(const FdArgs& a0, cudaStream_t s, int* nb) {
   constexpr int NC = NF + (GW ? 6 : 0);
+  FdArgs a = a0;
+  a.vec = (sizeof(R) == 4 && a.nx % 32 == 0) ? 1 : 0;  // whole 32-value rows, 16-byte aligned
+  const int wd = a.vec ? 40 : 34;
   dim3 block(32, a.ty);
   dim3 grid((a.nx + 31) / 32, (a.ny + a.ty - 1) / a.ty, (a.nz + a.zc - 1) / a.zc);
-  size_t smem = (size_t)3 * NC * 34 * (a.ty + 2) * sizeof(R);
-  if (34 * (a.ty + 2) > kFdMaxSlots * 32 * a.ty) return set_error(LAT_ERR_ARG, "FD tile too narrow");
+  size_t smem = (size_t)3 * NC * wd * (a.ty + 2) * sizeof(R);
+  if (a.ty < 1 || (!a.vec && 34 * (a.ty + 2) > kFdMaxSlots * 32 * a.ty))
+    return set_error(LAT_ERR_ARG, "FD tile too narrow");
   auto k = fd_kernel<R, KAHAN, NF, GW, SEVEN, MODE>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
