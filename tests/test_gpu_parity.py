@@ -83,6 +83,30 @@ def test_fd27_gw_minkowski(engine, orc, split):
     assert rel_err(Sg, So) <= 1e-9
 
 
+@pytest.mark.parametrize("shape", [(32, 16, 12), (64, 8, 8), (48, 8, 8)])
+def test_fd_fp32_tile_rows(engine, orc, shape):
+    """FP32-Kahan stencil passes against the FP64 oracle.  Rows of 32 and 64
+    sites are whole tiles (staged by 16-byte copies into padded rows); 48 has
+    a partial tile (4-byte copies).  FD27 with GW sourcing and FD7."""
+    nx, ny, nz = shape
+    for lap, gw in ((L.LAP_FD27, True), (L.LAP_FD7, False)):
+        c = L.make_config(shape, nfld=1, length=0.25 * nx, laplacian=lap, background=L.BG_MINKOWSKI,
+                          precision=L.FP32_KAHAN, model=L.MODEL_DOUBLE_WELL, model_params=(0.01,), gw=gw,
+                          gw_coupling=2.0)
+        g, o = pair(engine, orc, c)
+        same_start(g, o, mean=0.0, amp=0.3)
+        dt = 0.25 / 10
+        g.symp(2, dt, 12)
+        o.symp(2, dt, 12)
+        compare_state(g, o, 5e-6)
+        if gw:
+            gu, gpu_ = g.gw_state()
+            ou, opu = o.gw_state()
+            assert rel_err(gu, ou) <= 1e-4, rel_err(gu, ou)
+            assert rel_err(gpu_, opu) <= 1e-4, rel_err(gpu_, opu)
+        g.close()
+
+
 def test_fd27_conformal_plain_path(engine, orc):
     c = L.make_config(16, nfld=2, length=8.0, laplacian=L.LAP_FD27, background=L.BG_CONFORMAL,
                       model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
