@@ -152,6 +152,10 @@ struct lat_s {
   int cl_units = 0;  // 1: the network sees (a phi, pi / a) and predicts a^3 Delta
   double cl_tscale[2] = {1, 1};
   net::InferBufs cl_b{};
+  // the network runs on a side stream beside the kick's transforms (it reads
+  // the same fields, writes only cl_b), joined before the fused kick+drift
+  cudaStream_t cl_stream = nullptr;
+  cudaEvent_t cl_fork = nullptr, cl_join = nullptr;
 };
 
 namespace {
@@ -363,10 +367,13 @@ int exec_grav(lat_s* h, double hg) {
   return launch_grav(h->sc, hg, h->stream);
 }
 
-// corr: the attached closure's force enters the kick (spectral lattices)
-int exec_kd(lat_s* h, double hk, double hg, double hd, bool corr = false) {
+// corr: the attached closure's force enters the kick (spectral lattices);
+// join: an event of work on another stream the kick+drift waits for (after
+// the transforms of the Laplacian)
+int exec_kd(lat_s* h, double hk, double hg, double hd, bool corr = false, cudaEvent_t join = nullptr) {
   if (spectral(h)) {
     RET(spectral_lap(h, conformal(h)));
+    if (join) CK(cudaStreamWaitEvent(h->stream, join, 0));
     Timed t(h, LAT_K_KICKDRIFT);
     PwArgs a = pw_base(h);
     a.mode = PW_KD;
@@ -548,13 +555,28 @@ int exec_closure(lat_s* h, const std::vector<Op>& ops) {
   const bool fuse = spectral(h) && !(conf && h->cfg.split_order == LAT_SPLIT_DEFROST);
   const int fp64 = h->prec == LAT_FP64 ? 1 : 0;
   int kicks = 0;
-  auto infer = [&](double hg) -> int {  // before the kick with index `kicks`
-    if (kicks++ % h->cl_every) return LAT_OK;
-    Timed t(h, LAT_K_OTHER);
+  auto run_net = [&](double hg, cudaStream_t s) -> int {
     const size_t fb = (size_t)h->N * h->rsz;
     const void* ch[4] = {h->fld[h->cur], (const char*)h->fld[h->cur] + fb, h->fldp, (const char*)h->fldp + fb};
-    return net::infer(h->cl_net, ch, fp64, h->nx, h->ny, h->nz, h->cl_units ? h->sc : nullptr, hg, h->cl_b,
-                      h->stream);
+    return net::infer(h->cl_net, ch, fp64, h->nx, h->ny, h->nz, h->cl_units ? h->sc : nullptr, hg, h->cl_b, s);
+  };
+  auto infer = [&](double hg) -> int {  // before the kick with index `kicks`, in order
+    if (kicks++ % h->cl_every) return LAT_OK;
+    Timed t(h, LAT_K_OTHER);
+    return run_net(hg, h->stream);
+  };
+  // before a fused group: the network on the side stream, forked here; the
+  // event the group's kick+drift joins (null: nothing to join)
+  auto infer_side = [&](double hg, cudaEvent_t* join) -> int {
+    *join = nullptr;
+    if (h->timing || !h->cl_stream) return infer(hg);  // timed launches stay in order
+    if (kicks++ % h->cl_every) return LAT_OK;
+    CK(cudaEventRecord(h->cl_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->cl_stream, h->cl_fork, 0));
+    RET(run_net(hg, h->cl_stream));
+    CK(cudaEventRecord(h->cl_join, h->cl_stream));
+    *join = h->cl_join;
+    return LAT_OK;
   };
   size_t i = 0;
   while (i < ops.size()) {
@@ -562,15 +584,17 @@ int exec_closure(lat_s* h, const std::vector<Op>& ops) {
       double hd = 0;
       size_t j = i + 1;
       while (j < ops.size() && ops[j].t == 'D') hd += ops[j++].h;
-      RET(infer(0.0));
-      RET(exec_kd(h, ops[i].h, 0.0, hd, true));
+      cudaEvent_t join;
+      RET(infer_side(0.0, &join));
+      RET(exec_kd(h, ops[i].h, 0.0, hd, true, join));
       i = j;
       continue;
     }
     if (fuse && conf && ops[i].t == 'G' && i + 3 < ops.size() && ops[i + 1].t == 'K' && ops[i + 2].t == 'G' &&
         ops[i + 3].t == 'D' && ops[i].h == ops[i + 2].h) {
-      RET(infer(ops[i].h));
-      RET(exec_kd(h, ops[i + 1].h, ops[i].h, ops[i + 3].h, true));
+      cudaEvent_t join;
+      RET(infer_side(ops[i].h, &join));
+      RET(exec_kd(h, ops[i + 1].h, ops[i].h, ops[i + 3].h, true, join));
       i += 4;
       continue;
     }
@@ -924,8 +948,12 @@ int lat_destroy(lat_t* h) {
   if (!h) return LAT_OK;
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->cl_stream) cudaStreamSynchronize(h->cl_stream);
   free_graphs(h);
   if (h->cl_net) net::net_attach_ref(h->cl_net, -1);
+  if (h->cl_fork) cudaEventDestroy(h->cl_fork);
+  if (h->cl_join) cudaEventDestroy(h->cl_join);
+  if (h->cl_stream) cudaStreamDestroy(h->cl_stream);
   for (void* t : h->tw)
     if (t) cudaFree(t);
   {
@@ -1889,6 +1917,11 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
   if (every < 1) return set_error(LAT_ERR_ARG, "every must be >= 1");
   if (units != LAT_UNITS_PROGRAM && units != LAT_UNITS_CONFORMAL) return set_error(LAT_ERR_ARG, "units: 0 or 1");
   if (net::net_device(net) != h->dev) return set_error(LAT_ERR_ARG, "network and lattice on different devices");
+  if (!h->cl_stream) {
+    CK(cudaStreamCreateWithFlags(&h->cl_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->cl_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->cl_join, cudaEventDisableTiming));
+  }
   if (!h->cl_b.a0) {
     CK(cudaMalloc(&h->cl_b.a0, (size_t)h->N * net::C_IN * 2));
     CK(cudaMalloc(&h->cl_b.a1, (size_t)h->N * net::C_HID * 2));
