@@ -285,3 +285,32 @@ def test_closure_graphs_keyed_on_network_state(engine):
     renorm, _ = run(True, norm_b)  # prepared under norm_a: must not be replayed
     assert np.array_equal(renorm[0], fresh_b[0]) and np.array_equal(renorm[1], fresh_b[1])
     net.close()
+
+
+def test_closure_side_stream_matches_in_order(engine):
+    """The network runs on a side stream beside the kick's transforms and is
+    joined before the fused kick+drift; timed (eager, in-order) launches
+    must give the same bits.  Conformal background, conformal units (the
+    network sees a after the group's first gravity half-step)."""
+    c = L.make_config((32, 16, 16), nfld=2, length=16.0, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                      precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    f, p = random_state((2, 16, 16, 32), seed=21, mean=0.6, amp=0.2)
+    net = engine.Net(seed=8)
+    net.set_params(np.random.default_rng(3).standard_normal(net.nparams).astype(np.float32) * 0.05)
+    net.set_norm([0.5, 0.0, 0.0, 0.0], [1.0, 1.0, 1.0, 1.0], [1.5, 2.5])
+    out = []
+    for timed in (False, True):
+        g = engine.Lattice(c)
+        g.set_state(f, p)
+        g.set_scale_factor(1.0, 0.0)
+        g.calc_metric()
+        g.attach_closure(net, 2, L.UNITS_CONFORMAL)
+        g.timing(timed)
+        g.symp(4, 0.02, 5)
+        out.append((g.get_state(), g.scale_factor()))
+        g.attach_closure(None)
+        g.close()
+    (fa, pa), sa = out[0]
+    (fb, pb), sb = out[1]
+    assert np.array_equal(fa, fb) and np.array_equal(pa, pb) and sa == sb
+    net.close()
