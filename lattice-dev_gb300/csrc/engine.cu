@@ -814,7 +814,7 @@ const int kMaxBins = 2048;
 // a large mean keeps the digits of its fluctuation (an FP32 transform of
 // phi_hi alone would not).  Returns the precision of the spectrum written.
 int output_spectrum(lat_s* h, int what, int field, int slot, void** Fout, int* prec) {
-  const void* src;
+  const void* src = nullptr;
   RET(src_ptr(h, what, field, &src));
   if (h->prec == LAT_FP64) {
     void* F = (char*)h->Fk + (size_t)slot * h->M * h->csz;
@@ -1718,7 +1718,7 @@ namespace {
 std::string tune_key(lat_s* h) {
   cudaDeviceProp prop{};
   cudaGetDeviceProperties(&prop, h->dev);
-  char buf[256];
+  char buf[512];
   snprintf(buf, sizeof(buf), "%s|sm%d%d|p%d|lap%d|bg%d|nf%d|gw%d|%dx%dx%d|impl%d", prop.name, prop.major, prop.minor,
            h->prec, h->cfg.laplacian, h->cfg.background, h->nf, h->cfg.gw, h->nx, h->ny, h->nz,
            h->cfg.spectral_impl);

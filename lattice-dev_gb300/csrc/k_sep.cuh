@@ -393,7 +393,6 @@ __global__ void __launch_bounds__(256) sep_kernel(SepArgs a) {
   const R* __restrict__ phi = static_cast<const R*>(a.phi);
   const R* __restrict__ phic = static_cast<const R*>(a.phic);
   const R* __restrict__ pi = static_cast<const R*>(a.pi);
-  const R* __restrict__ lap = static_cast<const R*>(a.lap);
   R* __restrict__ phi_o = static_cast<R*>(a.phi_out);
   R* __restrict__ phic_o = static_cast<R*>(a.phic_out);
   R* __restrict__ pi_o = static_cast<R*>(a.pi_out);
