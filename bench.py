@@ -161,9 +161,10 @@ def max_over_ranks(pg, v):
 
 
 # ------------------------------------------------------------------ cpu leg
-def cpu_rate(steps_budget_s=20.0, max_steps=None, n=N_SIDE):
+def cpu_rate(steps_budget_s=20.0, max_steps=None, n=N_SIDE, warmup=1):
     """Times the CPU restatement (FP64, OpenMP on all host cores) on Yoshida-4
-    steps of the same workload; returns (site-updates/s, cores, steps)."""
+    steps of the same workload after `warmup` untimed steps; returns
+    (site-updates/s, cores, steps, seconds)."""
     import py_oracle
     L = importlib.import_module("lattice-dev_gb300")
     cores = os.cpu_count() or 1
@@ -172,7 +173,7 @@ def cpu_rate(steps_budget_s=20.0, max_steps=None, n=N_SIDE):
     o = py_oracle.Oracle(c)
     init_state(o, 1000)
     dt = c.len / n / 20
-    o.symp(4, dt, 1)  # warm-up (first-touch, FFT twiddles)
+    o.symp(4, dt, max(warmup, 1))  # warm-up (first-touch, FFT twiddles)
     done, t0 = 0, time.perf_counter()
     while True:
         o.symp(4, dt, 1)
@@ -194,15 +195,16 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": f"CPU restatement could not be built: {e}"}))
         return 0
     budget = float(os.environ.get("LAT_REF_BUDGET_S", "60"))
-    rate, cores, done, el = cpu_rate(steps_budget_s=budget, max_steps=max(args.steps, 1))
+    warm = max(args.warmup, 1)
+    rate, cores, done, el = cpu_rate(steps_budget_s=budget, max_steps=max(args.steps, 1), warmup=warm)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
-        "n_gpus": ws, "steps": done, "warmup": 1, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
+        "n_gpus": ws, "steps": done, "warmup": warm, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vacuum fluctuations)",
         "config": {"workload": "two-field preheating 256^3, L=10pi, spectral, Yoshida-4, conformal, dt=dx/20",
                    "global_batch": N_SIDE ** 3, "seq_len": 1, "parallelism": "replicas"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{done} Yoshida-4 steps of the 256^3 workload after 1 warm-up step "
+                         "sample": f"{done} Yoshida-4 steps of the 256^3 workload after {warm} warm-up steps "
                                    "(CPU restatement of the Fortran reference, FP64, OpenMP; the reference "
                                    "itself needs a Fortran compiler and FFTW, absent here)"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
