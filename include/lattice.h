@@ -243,6 +243,25 @@ int lat_gw_upload(lat_t* h, const double* u, const double* pu);
 int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0,
                     const double* dfld0, const double* m2eff, double amp,
                     double kcut_frac);
+/* The reference's own generator, sample(gamma, m2eff) of
+ * Pseudospec/openmp_dev/evolve_spectral.f90:421-506 as init_fields calls it
+ * (:294-299): per field f, fld = fld0[f] + sample(-1/4, m2eff) and
+ * fldp = dfld0[f] + sample(+1/4, m2eff), independent noise.  sample builds
+ * the radial profile k (k^2 + m2eff)^gamma exp(-(k/kcut)^2) (kcut = (n/2+1)
+ * dk/2) on an oversampled grid (16^2 points per lattice site along a side),
+ * takes its DST-II (FFTW's RODFT10), scales it by norm/k with
+ * norm = 0.5 / (n^3 sqrt(2 pi dk^3) mpl) (dkos/dxos), interpolates it onto
+ * every site's distance from the grid centre, multiplies each half-spectrum
+ * mode of its transform by Box-Muller noise sqrt(-2 ln a) e^{2 pi i p} and
+ * transforms back (unnormalised).  The noise is the counter-based draw of
+ * lat_init_vacuum keyed by (seed, 0x5300 + 2 f + {0 field, 1 momentum},
+ * mode) in place of the compiler's random_number, and the kx = 0 and
+ * kx = nx/2 planes are projected onto their Hermitian part before the
+ * inverse transform (a c2r of non-Hermitian input is FFT-library defined).
+ * Cubic lattices (LAT_ERR_UNSUPPORTED otherwise); mpl is the reference's
+ * mpl parameter (1e7/3 in hamiltonian_minkowski.f90:9). */
+int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0,
+                    const double* dfld0, double m2eff, double mpl);
 /* Thin-wall bubbles phi = -1 + sum_b [1 - tanh((r_b - R)/width)], zero momentum;
  * centres in lattice units of length (x,y,z per bubble).  Replaces
  * init_fields/initbubble, Discrete/Bubble-Collisions/ic_bubble.f90:17-123. */

@@ -104,6 +104,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_gw_spectrum": ([P, I, dp, dp], I), "lat_gw_download": ([P, dp, dp], I),
         "lat_gw_upload": ([P, dp, dp], I),
         "lat_init_vacuum": ([P, U64, dp, dp, dp, D, D], I), "lat_init_bubbles": ([P, I, dp, D, D], I),
+        "lat_init_sample": ([P, U64, dp, dp, D, D], I),
         "lat_init_bubbles_boosted": ([P, I, C.POINTER(I), D, D, D, D], I),
         "lat_checkpoint_write": ([P, C.c_char_p, D, I], I),
         "lat_checkpoint_read": ([P, C.c_char_p, dp, C.POINTER(I)], I),
@@ -335,6 +336,12 @@ class Lattice:
         m2 = np.ascontiguousarray(np.broadcast_to(np.asarray(m2eff, np.float64), (self.nfld,)))
         _check(_lib.lat_init_vacuum(self._h, C.c_uint64(seed), _dp(f0), _dp(d0), _dp(m2), amp, kcut_frac))
 
+
+    def init_sample(self, seed, fld0, dfld0, m2eff, mpl=1e7 / 3) -> None:
+        """The reference's sample() initial fields (lat_init_sample)."""
+        f0 = np.ascontiguousarray(np.broadcast_to(np.asarray(fld0, np.float64), (self.nfld,)))
+        d0 = np.ascontiguousarray(np.broadcast_to(np.asarray(dfld0, np.float64), (self.nfld,)))
+        _check(_lib.lat_init_sample(self._h, C.c_uint64(seed), _dp(f0), _dp(d0), float(m2eff), float(mpl)))
     def init_bubbles(self, centres, radius, width) -> None:
         c = np.ascontiguousarray(np.asarray(centres, np.float64).reshape(-1, 3))
         _check(_lib.lat_init_bubbles(self._h, c.shape[0], _dp(c), radius, width))

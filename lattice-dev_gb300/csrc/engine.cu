@@ -1495,6 +1495,87 @@ int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0, const double* d
   return rc;
 }
 
+int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0, const double* dfld0, double m2eff, double mpl) {
+  if (!h || !fld0 || !dfld0 || !(mpl != 0.0)) return set_error(LAT_ERR_ARG, "null or zero argument");
+  if (h->nx != h->ny || h->nx != h->nz) return set_error(LAT_ERR_UNSUPPORTED, "sample: cubic lattices");
+  ApiGuard g(h);
+  const int n = h->nx, os = 16, nos = n * os * os;
+  const double twopi = 6.2831853071795864769252867665590;
+  const double dk = twopi / (n * h->dx), dxos = h->dx / os, dkos = dk / (2.0 * os);
+  SampleArgs sa{};
+  sa.n = n;
+  sa.nos = nos;
+  sa.dkos = dkos;
+  sa.m2 = m2eff;
+  sa.kcut = (double)(n / 2 + 1) * dk / 2.0;
+  sa.norm = 0.5 / ((double)n * n * n * std::sqrt(twopi * dk * dk * dk) * mpl) * (dkos / dxos);
+  sa.M = h->M;
+  sa.seed = seed;
+  cufftHandle p1 = 0, p3 = 0, p3i = 0;
+  bool have1 = false, have3 = false, have3i = false;
+  int rc = LAT_OK;
+  do {
+    if (cudaMalloc(&sa.z, sizeof(double2) * 4 * (size_t)nos) != cudaSuccess ||
+        cudaMalloc(&sa.ker, sizeof(double) * nos) != cudaSuccess ||
+        cudaMalloc(&sa.f, sizeof(double) * h->N) != cudaSuccess ||
+        cudaMalloc(&sa.F, sizeof(double2) * h->M) != cudaSuccess) {
+      rc = set_error(LAT_ERR_ALLOC, "sample scratch");
+      break;
+    }
+    int dims[3] = {n, n, n};
+    size_t ws = 0;
+    bool ok = (have1 = cufftCreate(&p1) == CUFFT_SUCCESS) &&
+              cufftMakePlan1d(p1, 4 * nos, CUFFT_Z2Z, 1, &ws) == CUFFT_SUCCESS &&
+              cufftSetStream(p1, h->stream) == CUFFT_SUCCESS;
+    ok = ok && (have3 = cufftCreate(&p3) == CUFFT_SUCCESS) &&
+         cufftMakePlanMany(p3, 3, dims, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1, &ws) == CUFFT_SUCCESS &&
+         cufftSetStream(p3, h->stream) == CUFFT_SUCCESS;
+    ok = ok && (have3i = cufftCreate(&p3i) == CUFFT_SUCCESS) &&
+         cufftMakePlanMany(p3i, 3, dims, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2D, 1, &ws) == CUFFT_SUCCESS &&
+         cufftSetStream(p3i, h->stream) == CUFFT_SUCCESS;
+    if (!ok) {
+      rc = set_error(LAT_ERR_CUDA, "sample plans");
+      break;
+    }
+    for (int l = 0; l < h->nf && rc == LAT_OK; ++l) {
+      for (int kind = 0; kind < 2 && rc == LAT_OK; ++kind) {
+        sa.gamma = kind == 0 ? -0.25 : 0.25;
+        sa.stream = 0x5300 + 2 * l + kind;
+        if ((rc = launch_sample_steps(0, sa, h->stream))) break;
+        if (cufftExecZ2Z(p1, (cufftDoubleComplex*)sa.z, (cufftDoubleComplex*)sa.z, CUFFT_FORWARD) != CUFFT_SUCCESS) {
+          rc = set_error(LAT_ERR_CUDA, "sample dst");
+          break;
+        }
+        if ((rc = launch_sample_steps(1, sa, h->stream))) break;
+        if ((rc = launch_sample_steps(2, sa, h->stream))) break;
+        if (cufftExecD2Z(p3, sa.f, (cufftDoubleComplex*)sa.F) != CUFFT_SUCCESS) {
+          rc = set_error(LAT_ERR_CUDA, "sample d2z");
+          break;
+        }
+        if ((rc = launch_sample_steps(3, sa, h->stream))) break;
+        if ((rc = launch_sample_steps(4, sa, h->stream))) break;
+        if (cufftExecZ2D(p3i, (cufftDoubleComplex*)sa.F, sa.f) != CUFFT_SUCCESS) {
+          rc = set_error(LAT_ERR_CUDA, "sample z2d");
+          break;
+        }
+        if ((rc = launch_add_scale(sa.f, h->N, 1.0, kind == 0 ? fld0[l] : dfld0[l], h->stream))) break;
+        char* dst = (char*)(kind == 0 ? h->fld[h->cur] : h->fldp) + (size_t)l * h->N * h->rsz;
+        char* cdst = (kind == 0 && h->fldc) ? (char*)h->fldc + (size_t)l * h->N * h->rsz : nullptr;
+        rc = launch_from_fp64(sa.f, h->N, h->prec, dst, cdst, h->stream);
+      }
+    }
+    if (rc == LAT_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = set_error(LAT_ERR_CUDA, "sample sync");
+  } while (0);
+  cudaStreamSynchronize(h->stream);
+  if (have1) cufftDestroy(p1);
+  if (have3) cufftDestroy(p3);
+  if (have3i) cufftDestroy(p3i);
+  void* bufs[] = {sa.z, sa.ker, sa.f, sa.F};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  return rc;
+}
+
 int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres, double radius, double width) {
   if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(width > 0)) return set_error(LAT_ERR_ARG, "bad bubble arguments");
   ApiGuard g(h);

@@ -250,6 +250,21 @@ struct VacArgs {
 int launch_vacuum_modes(const VacArgs& a, cudaStream_t s);
 int launch_fd_laplacian64(const double* in, double* out, int nx, int ny, int nz, const double* lc, cudaStream_t s);
 int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStream_t s);
+// the reference's sample() IC, step by step (k_out.cu): 0 DST input, 1 DST
+// output (after the host's 4 nos FFT of z), 2 radial kernel on the lattice,
+// 3 noise (after the r2c of f into F), 4 Hermitian kx = 0, n/2 planes
+struct SampleArgs {
+  int n, nos;
+  double dkos, m2, gamma, kcut, norm;
+  double2* z;   // 4 nos
+  double* ker;  // nos
+  double* f;    // n^3
+  double2* F;   // (n/2 + 1) n^2
+  int64_t M;
+  uint64_t seed;
+  int stream;
+};
+int launch_sample_steps(int step, const SampleArgs& a, cudaStream_t s);
 int launch_bubbles(double* phi, int nx, int ny, int nz, double dx, int nbub, const double* centres_dev,
                    double radius, double width, cudaStream_t s);
 int launch_bubbles_boosted(double* phi, double* pi, int nx, int ny, int nz, double dx, int nbub, const int* cen,

@@ -410,6 +410,71 @@ __global__ void vacuum_kernel(VacArgs a) {
   }
 }
 
+// ------------------------------------------- the reference's sample() IC
+// (Pseudospec/openmp_dev/evolve_spectral.f90:421-506).  The DST-II of the
+// oversampled radial profile, Y_k = 2 sum_j X_j sin(pi (2j+1)(k+1) / (2 nos)),
+// is the imaginary part of one complex FFT of length 4 nos of the odd
+// embedding z[2j+1] = X_j, z[4 nos - 2j - 1] = -X_j: Y_k = -Im Z_{k+1}.
+__global__ void sample_dst_in_kernel(double2* z, int nos, double dkos, double m2, double gamma, double kcut) {
+  const int64_t L4 = 4LL * nos;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < L4; t += (int64_t)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    if (t & 1) {
+      const bool lower = t < 2LL * nos;
+      const int64_t j = lower ? (t - 1) / 2 : (L4 - t - 1) / 2;
+      const double kk = (j + 0.5) * dkos;
+      const double x = kk * pow(kk * kk + m2, gamma) * exp(-(kk / kcut) * (kk / kcut));
+      v = lower ? x : -x;
+    }
+    z[t] = make_double2(v, 0.0);
+  }
+}
+
+// ker[k] = norm Y_k / (k + 1): the 1-based profile ker(k + 1)
+__global__ void sample_dst_out_kernel(const double2* Z, int nos, double norm, double* ker) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nos; t += gridDim.x * blockDim.x)
+    ker[t] = norm * (-Z[t + 1].y) / (t + 1);
+}
+
+// the profile interpolated at |(i, j, k) - nn| os (1-based indices, nn = n/2 + 1)
+__global__ void sample_kernel3d(const double* ker, int n, double* f) {
+  const int64_t N = (int64_t)n * n * n;
+  const int nn = n / 2 + 1, os = 16;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % n), y = (int)((t / n) % n), z = (int)(t / ((int64_t)n * n));
+    const double di = x + 1 - nn, dj = y + 1 - nn, dz = z + 1 - nn;
+    const double kk = sqrt(di * di + dj * dj + dz * dz) * os;
+    const int l = (int)floor(kk);
+    f[t] = l > 0 ? ker[l - 1] + (kk - l) * (ker[l] - ker[l - 1]) : (4.0 * ker[0] - ker[1]) / 3.0;
+  }
+}
+
+// every half-spectrum mode times the Box-Muller noise of its counter-based draw
+__global__ void sample_noise_kernel(double2* F, int64_t M, uint64_t seed, int stream) {
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+    const double2 g = mode_gauss(seed, stream, m), v = F[m];
+    F[m] = make_double2(v.x * g.x - v.y * g.y, v.x * g.y + v.y * g.x);
+  }
+}
+
+// the kx = 0 and kx = n/2 planes projected onto their Hermitian part
+__global__ void sample_hermitize_kernel(double2* F, int n) {
+  const int hx = n / 2 + 1;
+  const int64_t P = 2LL * n * n;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < P; t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (t < (int64_t)n * n) ? 0 : n / 2;
+    const int64_t r = t % ((int64_t)n * n);
+    const int y = (int)(r % n), z = (int)(r / n);
+    const int64_t m = ((int64_t)z * n + y) * hx + x;
+    const int64_t mp = ((int64_t)((n - z) % n) * n + (n - y) % n) * hx + x;
+    if (mp < m) continue;
+    const double2 a = F[m], b = F[mp];
+    const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    F[m] = h;
+    F[mp] = make_double2(h.x, -h.y);
+  }
+}
+
 // STENCIL(c,LAPLACE) with pre-scaled coefficients lc = c/(cc dx^2), FP64.
 __global__ void fd_lap64_kernel(const double* g, double* out, int nx, int ny, int nz, double l0, double l1, double l2,
                                 double l3) {
@@ -582,6 +647,22 @@ int launch_fd_laplacian64(const double* in, double* out, int nx, int ny, int nz,
   fd_lap64_kernel<<<grid_for((int64_t)nx * ny * nz), 256, 0, s>>>(in, out, nx, ny, nz, lc[0], lc[1], lc[2], lc[3]);
   return done("fd laplacian");
 }
+int launch_sample_steps(int step, const SampleArgs& a, cudaStream_t s) {
+  const int blk = 256;
+  auto grid = [&](int64_t n) { return (unsigned)std::min<int64_t>((n + blk - 1) / blk, 4096); };
+  switch (step) {
+    case 0: sample_dst_in_kernel<<<grid(4LL * a.nos), blk, 0, s>>>(a.z, a.nos, a.dkos, a.m2, a.gamma, a.kcut); break;
+    case 1: sample_dst_out_kernel<<<grid(a.nos), blk, 0, s>>>(a.z, a.nos, a.norm, a.ker); break;
+    case 2: sample_kernel3d<<<grid((int64_t)a.n * a.n * a.n), blk, 0, s>>>(a.ker, a.n, a.f); break;
+    case 3: sample_noise_kernel<<<grid(a.M), blk, 0, s>>>(a.F, a.M, a.seed, a.stream); break;
+    case 4: sample_hermitize_kernel<<<grid(2LL * a.n * a.n), blk, 0, s>>>(a.F, a.n); break;
+    default: return set_error(LAT_ERR_ARG, "sample step");
+  }
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "sample launch");
+}
+
 int launch_add_scale(double* f, int64_t n, double scale, double offset, cudaStream_t s) {
   add_scale_kernel<<<grid_for(n), 256, 0, s>>>(f, n, scale, offset);
   return done("add_scale");

@@ -725,6 +725,85 @@ int orc_init_vacuum(orc_t* o, uint64_t seed, const double* fld0, const double* d
   return LAT_OK;
 }
 
+// The reference's sample(gamma, m2eff) (Pseudospec/openmp_dev/evolve_spectral.f90:
+// 421-506): a radial profile ker(k) = k (k^2 + m2eff)^gamma exp(-(k/kcut)^2) on
+// an oversampled grid (os = 16, nos = n os^2 points, dk/(2 os) apart), its
+// DST-II (FFTW RODFT10: Y_k = 2 sum_j X_j sin(pi (j + 1/2)(k + 1)/nos), here
+// summed directly), scaled by norm / k, interpolated linearly onto the
+// radius |(i, j, k) - nn| os of every site about the grid centre
+// nn = n/2 + 1 (1-based), transformed (r2c), every half-spectrum mode times
+// Box-Muller noise sqrt(-2 ln a) e^{2 pi i p}, and transformed back
+// (unnormalised).  The noise is the counter-based draw of orc_mode_gauss on
+// stream 0x5300 + 2 field + (0 field, 1 momentum) (Fortran's random_number
+// cannot be reproduced); the kx = 0 and kx = nx/2 planes are projected onto
+// their Hermitian part before the inverse transform (a c2r of non-Hermitian
+// input is FFT-library defined).  Cubic lattices; norm uses mpl.
+static void sample_field(orc_t* o, uint64_t seed, int stream, double gamma, double m2eff, double mpl, double* out) {
+  const int n = o->nx, os = 16, nos = n * os * os, nn = n / 2 + 1, hx = n / 2 + 1;
+  const double twopi = 6.2831853071795864769252867665590, pi = twopi / 2;
+  const double dx = o->dx, dk = twopi / (n * dx), dxos = dx / os, dkos = dk / (2.0 * os);
+  const double kcut = (double)nn * dk / 2.0;
+  const double nvol = (double)n * n * n;
+  const double norm = 0.5 / (nvol * std::sqrt(twopi * dk * dk * dk) * mpl) * (dkos / dxos);
+  std::vector<double> X(nos), ker(nos);
+  for (int j = 0; j < nos; ++j) {
+    const double kk = (j + 0.5) * dkos;
+    X[j] = kk * std::pow(kk * kk + m2eff, gamma) * std::exp(-(kk / kcut) * (kk / kcut));
+  }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nos; ++k) {
+    double y = 0.0;
+    // angle pi (2j + 1)(k + 1) / (2 nos), reduced modulo 2 pi in integers
+    for (int j = 0; j < nos; ++j)
+      y += X[j] * std::sin(pi * (double)(((int64_t)(2 * j + 1) * (k + 1)) % (4 * (int64_t)nos)) / (2.0 * nos));
+    ker[k] = norm * (2.0 * y) / (k + 1);  // ker(k + 1) of the 1-based profile
+  }
+  std::vector<double> f(o->N);
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < n; ++z)
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < n; ++x) {
+        const double di = x + 1 - nn, dj = y + 1 - nn, dz = z + 1 - nn;
+        const double kk = std::sqrt(di * di + dj * dj + dz * dz) * os;
+        const int l = (int)std::floor(kk);
+        f[idx3(x, y, z, n, n)] = l > 0 ? ker[l - 1] + (kk - l) * (ker[l] - ker[l - 1]) : (4.0 * ker[0] - ker[1]) / 3.0;
+      }
+  std::vector<cplx> F(o->M);
+  o->fft->r2c(f.data(), F.data());
+  for (int64_t m = 0; m < o->M; ++m) {
+    double g[2];
+    orc_mode_gauss(seed, stream, m, g);
+    F[m] *= cplx(g[0], g[1]);
+  }
+  for (int z = 0; z < n; ++z)
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < hx; x += (n / 2 > 0 ? n / 2 : 1)) {
+        if (x != 0 && 2 * x != n) continue;
+        const int64_t m = ((int64_t)z * n + y) * hx + x;
+        const int64_t mp = ((int64_t)((n - z) % n) * n + (n - y) % n) * hx + x;
+        if (mp < m) continue;
+        const cplx h = 0.5 * (F[m] + std::conj(F[mp]));
+        F[m] = h;
+        F[mp] = std::conj(h);
+      }
+  o->fft->c2r(F.data(), out);
+}
+
+int orc_init_sample(orc_t* o, uint64_t seed, const double* fld0, const double* dfld0, double m2eff, double mpl) {
+  if (o->nx != o->ny || o->nx != o->nz) return LAT_ERR_UNSUPPORTED;
+  for (int l = 0; l < o->nf; ++l) {
+    double* f = &o->fld[l * o->N];
+    double* p = &o->fldp[l * o->N];
+    sample_field(o, seed, 0x5300 + 2 * l, -0.25, m2eff, mpl, f);
+    sample_field(o, seed, 0x5300 + 2 * l + 1, 0.25, m2eff, mpl, p);
+    for (int64_t s = 0; s < o->N; ++s) {
+      f[s] += fld0[l];
+      p[s] += dfld0[l];
+    }
+  }
+  return LAT_OK;
+}
+
 int orc_init_bubbles(orc_t* o, int32_t nbub, const double* centres, double radius, double width) {
 #pragma omp parallel for schedule(static)
   for (int z = 0; z < o->nz; ++z)

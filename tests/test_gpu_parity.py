@@ -184,6 +184,32 @@ def test_vacuum_ic_identical(engine, orc):
     compare_state(g, o, 1e-12)
 
 
+@pytest.mark.parametrize("n,prec", [(16, L.FP64), (32, L.FP64), (32, L.FP32_KAHAN)])
+def test_sample_ic_matches_oracle(engine, orc, n, prec):
+    """The reference's sample() generator (DST-II of the oversampled radial
+    profile through a length-4 nos FFT, noise per mode) against the oracle,
+    whose DST is the direct sum; fluctuations compared relative to their size."""
+    c = two_field_spectral(n, prec)
+    g, o = pair(engine, orc, c)
+    fld0, dfld0 = [1.0, 0.25], [0.1, -0.2]
+    g.init_sample(77, fld0, dfld0, 3.0, mpl=0.5)
+    o.init_sample(77, fld0, dfld0, 3.0, mpl=0.5)
+    gf, gp = g.get_state()
+    of, op = o.get_state()
+    tol = 1e-10 if prec == L.FP64 else 1e-6
+    for l in range(2):
+        df, dp_ = of[l] - fld0[l], op[l] - dfld0[l]
+        assert np.max(np.abs(gf[l] - of[l])) <= tol * np.max(np.abs(df)) + 1e-15
+        assert np.max(np.abs(gp[l] - op[l])) <= tol * np.max(np.abs(dp_)) + 1e-15
+        assert np.std(df) > 0 and np.std(dp_) > 0
+    if n == 16:  # cubic lattices only
+        nc = L.make_config((16, 16, 8), nfld=2, length=4.0, laplacian=L.LAP_SPECTRAL)
+        h = engine.Lattice(nc)
+        with pytest.raises(engine.LatticeError):
+            h.init_sample(1, [0, 0], [0, 0], 1.0)
+        h.close()
+
+
 def test_energies(engine, orc):
     for c in (phi4_fd7(16), bubble_fd27(12), two_field_spectral(16, conformal=True)):
         g, o = pair(engine, orc, c)

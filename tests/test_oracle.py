@@ -211,3 +211,65 @@ def test_yoshida_weights_golden():
     w0, w1 = g["w4"]
     assert abs(w0 + 2 * w1 - 1) < 1e-15
     assert abs(2 * w1 ** 3 + w0 ** 3) < 1e-14  # third-order condition of the 4th-order composition
+
+
+def _np_mode_gauss(seed, stream, modes):
+    """The counter-based Box-Muller draw of orc_mode_gauss, in numpy uint64."""
+    def mix(z):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+    with np.errstate(over="ignore"):
+        k0 = mix(mix(np.uint64(seed)) ^ np.uint64(stream))
+        key = mix(k0 ^ modes.astype(np.uint64))
+        u1 = ((mix(key ^ np.uint64(1)) >> np.uint64(11)).astype(np.float64) + 1.0) / 2.0 ** 53
+        u2 = ((mix(key ^ np.uint64(2)) >> np.uint64(11)).astype(np.float64) + 1.0) / 2.0 ** 53
+    r = np.sqrt(-2.0 * np.log(u1))
+    return r * np.exp(2j * np.pi * u2)
+
+
+def _np_sample(n, dx, seed, stream, gamma, m2eff, mpl):
+    """sample(gamma, m2eff) of Pseudospec/openmp_dev/evolve_spectral.f90:421-506
+    with scipy's DST-II (FFTW's RODFT10) and numpy FFTs; noise and the
+    Hermitian projection of the kx = 0 and nx/2 planes as the oracle's."""
+    from scipy import fft as sfft
+    os_, nn = 16, n // 2 + 1
+    nos = n * os_ * os_
+    dk = 2 * np.pi / (n * dx)
+    dxos, dkos, kcut = dx / os_, dk / (2 * os_), nn * dk / 2
+    norm = 0.5 / (float(n) ** 3 * np.sqrt(2 * np.pi * dk ** 3) * mpl) * (dkos / dxos)
+    kk = (np.arange(nos) + 0.5) * dkos
+    ker = norm * sfft.dst(kk * (kk ** 2 + m2eff) ** gamma * np.exp(-(kk / kcut) ** 2), type=2) / np.arange(1, nos + 1)
+    i = np.arange(n) + 1 - nn
+    r = np.sqrt(i[None, None, :] ** 2 + i[None, :, None] ** 2 + i[:, None, None] ** 2) * os_
+    l = np.floor(r).astype(np.int64)
+    lo = ker[np.maximum(l, 1) - 1]
+    f = np.where(l > 0, lo + (r - l) * (ker[np.minimum(l, nos - 1)] - lo), (4 * ker[0] - ker[1]) / 3)
+    F = np.fft.rfftn(f)  # [z][y][x/2+1]
+    F *= _np_mode_gauss(seed, stream, np.arange(F.size)).reshape(F.shape)
+    for x in (0, n // 2):
+        P = F[:, :, x]
+        Q = np.conj(P[(-np.arange(n)) % n][:, (-np.arange(n)) % n])
+        F[:, :, x] = 0.5 * (P + Q)
+    return np.fft.irfftn(F, s=(n, n, n), axes=(0, 1, 2)) * n ** 3
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_sample_ic_matches_numpy(orc, n):
+    """The oracle's restatement of the reference's sample() IC (oversampled
+    DST-II radial kernel, Box-Muller noise per mode) against scipy/numpy."""
+    c = L.make_config(n, nfld=2, length=2.5 * n / 8, laplacian=L.LAP_SPECTRAL, model=L.MODEL_PHI4_G2,
+                      model_params=(1.0, 2.0))
+    o = orc.Oracle(c)
+    fld0, dfld0, m2, mpl = [1.0, 0.2], [0.0, -0.1], 3.0, 0.5
+    o.init_sample(1234, fld0, dfld0, m2, mpl)
+    f, p = o.get_state()
+    dx = c.len / n
+    for l in range(2):
+        wf = fld0[l] + _np_sample(n, dx, 1234, 0x5300 + 2 * l, -0.25, m2, mpl)
+        wp = dfld0[l] + _np_sample(n, dx, 1234, 0x5300 + 2 * l + 1, 0.25, m2, mpl)
+        assert np.max(np.abs(f[l] - wf)) <= 1e-9 * np.max(np.abs(wf - fld0[l]))
+        assert np.max(np.abs(p[l] - wp)) <= 1e-9 * np.max(np.abs(wp - dfld0[l]))
+        assert np.std(f[l]) > 0 and np.std(p[l]) > 0
