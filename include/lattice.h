@@ -294,6 +294,16 @@ int lat_checkpoint_read(lat_t* h, const char* dir, double* time, int32_t* frame)
  * <phi_1>, <phi_2> (the last for two or more fields), each as Fortran
  * ES22.15 followed by two spaces. */
 int lat_write_energy_line(lat_t* h, const char* path, double time);
+/* One record of the DEFROST tree's LOG.out (output_log_file,
+ * Discrete/Bubble-Collisions/iofile.f90:614-630), appended to `path` in the
+ * format of lat_write_energy_line, after a one-line header when the file is
+ * empty: t, a, H, <rho> = KE + GE + PE (scalar_en), rhoball, KE, PE,
+ * GE (grad_en), GE (grad_en_wlap), -3H^2 (grav_en), KE + GE + PE - 3H^2
+ * (hamiltonian).  rhoball (iofile.f90:523-567) sums ekin (sum_f pi_f)^2 +
+ * egrad GRAD2 + V over the sites with |(i, j, k) - n/2|^2 dx^2 < 45 (1-based
+ * indices), ekin = 1/(2 a^6), egrad = 1/(4 (a dx)^2 cc).  Finite-difference
+ * lattices (LAT_ERR_UNSUPPORTED otherwise). */
+int lat_write_log_line(lat_t* h, const char* path, double time);
 /* Appends one block to a spectrum file as make_output writes it
  * (evolve_spectral.f90:525-549, spectrum.out): for each of the ns bins,
  * (i-1) dk, P(phi_1), P(pi_1), Re and Im of the pi_1 x conj(phi_1) cross

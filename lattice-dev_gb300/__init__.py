@@ -133,6 +133,7 @@ def _declare(lib: C.CDLL) -> None:
         "lat_net_train_step": ([P, P, I64, C.POINTER(I), I, I, I, I, D, dp], I),
         "lat_net_launch_count": ([P], I64), "lat_net_time_forward": ([P, I, I, I, I, dp], I),
         "lat_write_energy_line": ([P, C.c_char_p, D], I), "lat_write_spectrum_block": ([P, C.c_char_p], I),
+        "lat_write_log_line": ([P, C.c_char_p, D], I),
         "lat_closure_attach": ([P, P, I, I], I), "lat_coarsen": ([P, I, I, P], I),
     }
     for name, (args, res) in sig.items():
@@ -412,6 +413,10 @@ class Lattice:
 
     def write_energy_line(self, path, time: float) -> None:
         _check(_lib.lat_write_energy_line(self._h, str(path).encode(), time))
+
+    def write_log_line(self, path, time: float) -> None:
+        """One LOG.out record of the DEFROST tree (lat_write_log_line)."""
+        _check(_lib.lat_write_log_line(self._h, str(path).encode(), time))
 
     def write_spectrum_block(self, path) -> None:
         _check(_lib.lat_write_spectrum_block(self._h, str(path).encode()))

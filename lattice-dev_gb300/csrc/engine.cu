@@ -721,8 +721,11 @@ int read_scalars(lat_s* h, DevScalars* out) {
   return LAT_OK;
 }
 
-int compute_energies(lat_s* h, double* out) {
+// ball_r2 > 0 (FD lattices): also the sums of LOG.out's rhoball into ball[3]
+int compute_energies(lat_s* h, double* out, double ball_r2 = 0.0, double* ball = nullptr) {
   EnergyArgs e{};
+  e.ball_r2 = spectral(h) ? 0.0 : ball_r2;
+  e.dx = h->dx;
   e.nx = h->nx; e.ny = h->ny; e.nz = h->nz; e.nf = h->nf;
   e.phi = h->fld[h->cur];
   e.phic = h->fldc;
@@ -770,6 +773,11 @@ int compute_energies(lat_s* h, double* out) {
   out[LAT_E_MEAN0] = s.red[2] / Nd;
   out[LAT_E_MEAN1] = s.red[3] / Nd;
   out[LAT_E_GW] = h->cfg.gw ? 0.5 * (s.red[6] + s.red[7] * elap) / Nd : 0.0;
+  if (ball) {
+    ball[0] = s.red[9];
+    ball[1] = s.red[10];
+    ball[2] = s.red[11];
+  }
   return LAT_OK;
 }
 
@@ -2113,6 +2121,30 @@ int lat_write_energy_line(lat_t* h, const char* path, double time) {
                            e[LAT_E_MEAN0], e[LAT_E_MEAN1]};
   const int n = h->nf >= 2 ? 11 : 10;
   for (int i = 0; i < n; ++i) put_es(fp, cols[i]);
+  fputc('\n', fp);
+  const bool ok = fclose(fp) == 0;
+  return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);
+}
+
+int lat_write_log_line(lat_t* h, const char* path, double time) {
+  if (!h || !path) return set_error(LAT_ERR_ARG, "null argument");
+  ApiGuard g(h);
+  if (spectral(h)) return set_error(LAT_ERR_UNSUPPORTED, "LOG.out: finite-difference lattices");
+  double e[LAT_NENERGY], ball[3];
+  RET(compute_energies(h, e, 45.0, ball));  // ballrad = 5 3^2 (iofile.f90:527)
+  const double a = e[LAT_E_A], ap = e[LAT_E_AP];
+  const double H = conformal(h) ? -ap / 6.0 / (a * a) : 0.0;
+  // get_energy_coeffs (homlat.f90:34-46): ekin (sum pi)^2 + egrad GRAD2 + epot modelv
+  const double ekin = 0.5 / std::pow(a, 6), egrad = 0.25 / (a * h->dx) / (a * h->dx) / h->c[4];
+  const double rhoball = ekin * ball[0] + egrad * ball[1] + ball[2];
+  const double ke = e[LAT_E_KE], pe = e[LAT_E_PE], ge = e[LAT_E_GE_GRAD], gel = e[LAT_E_GE_LAP];
+  const double grav = e[LAT_E_GRAV];
+  FILE* fp = fopen(path, "a");
+  if (!fp) return set_error(LAT_ERR_IO, std::string("cannot open ") + path);
+  if (ftell(fp) == 0)
+    fputs("# t  a  H  <rho>  rhoball  KE  PE  GE  GE(lap)  -3H^2  H_total\n", fp);
+  const double cols[11] = {time, a, H, ke + ge + pe, rhoball, ke, pe, ge, gel, grav, ge + ke + pe + grav};
+  for (double v : cols) put_es(fp, v);
   fputc('\n', fp);
   const bool ok = fclose(fp) == 0;
   return ok ? LAT_OK : set_error(LAT_ERR_IO, std::string("write failed: ") + path);

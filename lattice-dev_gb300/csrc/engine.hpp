@@ -227,6 +227,10 @@ struct EnergyArgs {
   const void* pu;
   int fd;  // FD sums [4],[5],[7]
   double c[4];  // raw stencil coefficients c0..c3
+  // FD only, ball_r2 > 0: over the sites with |(x, y, z) + 1 - n/2|^2 dx^2 <
+  // ball_r2 (LOG.out's rhoball), sum (sum_f pi_f)^2, the stencil's gradient
+  // squared and V into red[9], red[10], red[11]
+  double ball_r2, dx;
   ModelP model;
   DevScalars* sc;
   RedBuf rb;

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
   const R* u = static_cast<const R*>(a.u);
   const R* pu = static_cast<const R*>(a.pu);
   using Acc = typename AccOf<R>::type;
-  Acc s[8];
+  Acc s[11];
   const R c0 = (R)a.c[0], c1 = (R)a.c[1], c2 = (R)a.c[2], c3 = (R)a.c[3];
   int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if constexpr (sizeof(R) == 4) {
@@ -291,12 +291,25 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
         grad2 = c1 * q1 + c2 * q2 + c3 * q3;
       };
       if (a.fd) {
+        R g2sum = 0;
 #pragma unroll
         for (int l = 0; l < NF; ++l) {
           R ls, g2;
           stencil(phi + l * N, ls, g2);
           s[4].add(-f[l] * ls);
           s[5].add(g2);
+          g2sum += g2;
+        }
+        if (a.ball_r2 > 0.0) {  // 1-based indices about n/2 (iofile.f90:552)
+          const double bx = x + 1 - nx / 2, by = y + 1 - ny / 2, bz = z + 1 - nz / 2;
+          if ((bx * bx + by * by + bz * bz) * a.dx * a.dx < a.ball_r2) {
+            R psum = 0;
+#pragma unroll
+            for (int l = 0; l < NF; ++l) psum += pi[l * N + t];
+            s[8].add(psum * psum);
+            s[9].add(g2sum);
+            s[10].add(model_v<R, NF>(a.model, f));
+          }
         }
       }
       if (u) {
@@ -311,13 +324,13 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
       }
     }
   }
-  typename Acc::Red v[8];
-  double tot[8];
+  typename Acc::Red v[11];
+  double tot[11];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = s[i].red();
-  if (grid_reduce<8>(v, a.rb, tot)) {
-    for (int i = 0; i < 8; ++i) {
-      a.sc->red[i] = tot[i];
+  for (int i = 0; i < 11; ++i) v[i] = s[i].red();
+  if (grid_reduce<11>(v, a.rb, tot)) {
+    for (int i = 0; i < 11; ++i) {
+      a.sc->red[i < 8 ? i : i + 1] = tot[i];  // red[8] is the spectral Parseval sum
       if (bad(tot[i])) a.sc->err |= 1u;
     }
   }

@@ -574,6 +574,33 @@ int orc_laplacian(orc_t* o, int32_t field, double* out) {
   return LAT_OK;
 }
 int orc_energies(orc_t* o, double* out) { energies(*o, out); return LAT_OK; }
+
+// LOG.out's rhoball (Discrete/Bubble-Collisions/iofile.f90:523-567): over
+// the sites with ((i - n/2)^2 + (j - n/2)^2 + (k - n/2)^2) dx^2 < r2
+// (1-based indices) the sums of (sum_f fldp_f)^2, STENCIL(c, GRAD2) summed
+// over the fields, and V, into out[0..2].
+int orc_rho_ball_sums(orc_t* o, double r2, double* out) {
+  double T = 0, G = 0, V = 0;
+  for (int z = 0; z < o->nz; ++z)
+    for (int y = 0; y < o->ny; ++y)
+      for (int x = 0; x < o->nx; ++x) {
+        const double bx = x + 1 - o->nx / 2, by = y + 1 - o->ny / 2, bz = z + 1 - o->nz / 2;
+        if ((bx * bx + by * by + bz * bz) * o->dx * o->dx >= r2) continue;
+        const int64_t s = idx3(x, y, z, o->nx, o->ny);
+        double psum = 0, f[8];
+        for (int l = 0; l < o->nf; ++l) {
+          psum += o->fldp[l * o->N + s];
+          G += stencil_grad2(*o, &o->fld[l * o->N], x, y, z);
+        }
+        T += psum * psum;
+        site_fields(*o, s, f);
+        V += potential(*o, f);
+      }
+  out[0] = T;
+  out[1] = G;
+  out[2] = V;
+  return LAT_OK;
+}
 int orc_spectrum_nbins(orc_t* o, int32_t* ns) { *ns = nbins_ref(*o); return LAT_OK; }
 
 int orc_spectrum(orc_t* o, int32_t what, int32_t field, int32_t mode, int32_t nbins, double* S, double* W) {

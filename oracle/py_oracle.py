@@ -52,7 +52,7 @@ def load() -> C.CDLL:
         "orc_spectrum": ([P, I, I, I, I, dp, dp], I), "orc_crossspec": ([P, I, I, I, I, I, dp, dp], I),
         "orc_gw_spectrum": ([P, I, dp, dp], I), "orc_mode_gauss": ([U64, I, C.c_int64, dp], I),
         "orc_init_vacuum": ([P, U64, dp, dp, dp, D, D], I), "orc_init_bubbles": ([P, I, dp, D, D], I),
-        "orc_init_sample": ([P, U64, dp, dp, D, D], I),
+        "orc_init_sample": ([P, U64, dp, dp, D, D], I), "orc_rho_ball_sums": ([P, D, dp], I),
         "orc_fft_r2c_3d": ([I, I, I, dp, dp], I), "orc_fft_c2r_3d": ([I, I, I, dp, dp], I),
     }
     for name, (args, res) in sig.items():
@@ -177,6 +177,11 @@ class Oracle:
         d0 = np.ascontiguousarray(np.broadcast_to(np.asarray(dfld0, np.float64), (self.nfld,)))
         m2 = np.ascontiguousarray(np.broadcast_to(np.asarray(m2eff, np.float64), (self.nfld,)))
         _check(_lib.orc_init_vacuum(self._h, C.c_uint64(seed), _dp(f0), _dp(d0), _dp(m2), amp, kcut_frac))
+
+    def rho_ball_sums(self, r2=45.0):
+        out = np.zeros(3)
+        _check(_lib.orc_rho_ball_sums(self._h, float(r2), _dp(out)))
+        return out
 
     def init_sample(self, seed, fld0, dfld0, m2eff, mpl=1e7 / 3):
         f0 = np.ascontiguousarray(np.broadcast_to(np.asarray(fld0, np.float64), (self.nfld,)))

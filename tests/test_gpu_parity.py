@@ -443,6 +443,41 @@ def test_output_cube_bov(engine, tmp_path, prec):
         g.write_cube(L.SPEC_FLD, 0, 3, tmp_path, "fld", 1, 0.0)  # 16 is not a multiple of 3
 
 
+def test_log_out_record(engine, orc, tmp_path):
+    """LOG.out of the DEFROST tree (output_log_file, iofile.f90:614-630): t, a,
+    H, <rho>, rhoball, KE, PE, GE, GE(lap), -3H^2, hamiltonian, with rhoball
+    summed over the sites within sqrt(45) of the grid centre."""
+    c = L.make_config(32, nfld=2, length=32.0, laplacian=L.LAP_FD27, background=L.BG_CONFORMAL,
+                      model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0))
+    g, o = pair(engine, orc, c)
+    same_start(g, o, mean=0.5, amp=0.2)
+    for obj in (g, o):
+        obj.set_scale_factor(1.3, -0.7)
+    path = tmp_path / "LOG.out"
+    g.write_log_line(path, 2.5)
+    g.write_log_line(path, 2.5)
+    lines = path.read_text().splitlines()
+    assert lines[0].startswith("#") and len(lines) == 3
+    rows = [np.array([float(v) for v in ln.split()]) for ln in lines[1:]]
+    assert np.array_equal(rows[0], rows[1]) and rows[0].size == 11
+    e = o.energies()
+    a, ap = 1.3, -0.7
+    H = -ap / 6.0 / a ** 2
+    T, G, V = o.rho_ball_sums(45.0)
+    dx = 1.0
+    cc = 30.0  # the 27-point stencil's normalisation
+    rhoball = 0.5 / a ** 6 * T + 0.25 / (a * dx) ** 2 / cc * G + V
+    ke, pe, ge, gel = e[L.E_KE], e[L.E_PE], e[L.E_GE_GRAD], e[L.E_GE_LAP]
+    want = [2.5, a, H, ke + ge + pe, rhoball, ke, pe, ge, gel, -3 * H * H, ge + ke + pe - 3 * H * H]
+    assert 0 < T and 0 < G
+    for i, (got, w) in enumerate(zip(rows[0], want)):
+        assert abs(got - w) <= 1e-10 * max(abs(w), 1e-300), (i, got, w)
+    spec = engine.Lattice(two_field_spectral(16))
+    with pytest.raises(engine.LatticeError):
+        spec.write_log_line(tmp_path / "x.out", 0.0)
+    spec.close()
+
+
 def test_output_files_reference_layout(engine, tmp_path):
     """energy_spec.out and spectrum.out records in the reference's column
     layout (ES22.15 + 2X fields), with the values of the engine's reductions."""
