@@ -39,7 +39,7 @@ enum lat_status {
   LAT_ERR_ALLOC = 5,       /* device or host allocation failed             */
   LAT_ERR_STATE = 6,       /* call not valid in the handle's state         */
   LAT_ERR_IO = 7,          /* checkpoint file error                        */
-  LAT_ERR_UNSUPPORTED = 8  /* valid request this build does not implement  */
+  LAT_ERR_UNSUPPORTED = 8  /* valid request the engine does not implement   */
 };
 
 /* ---------------------------------------------------------- configuration */

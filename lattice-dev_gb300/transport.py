@@ -7,9 +7,9 @@ Discrete/Bubble-Collisions/scafld.f90:120-192) and MPI_Allreduce of the
 lattice sums that feed the Friedmann update (hamiltonian_conformal.f90:112-114,
 198-201).  This module is that layer for GB300 machines: a ``Transport``
 interface (implemented over torch.distributed: NCCL between GPUs, gloo between
-CPU ranks for tests), a z-slab decomposition and the halo exchange.  One box
-in this build has one GPU, so the engine runs replicas there; the exchange
-logic is exercised by CPU ranks.
+CPU ranks for tests), a z-slab decomposition and the halo exchange.  On a
+machine with one GPU the engine runs replicas; the exchange logic is
+exercised by CPU ranks.
 """
 from __future__ import annotations
 

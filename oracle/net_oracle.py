@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY: CPU FP64 restatement of the closure network.
 
-Checker for the GPU closure kernels (BF16 tensor-core convolutions): the same
+Reference values for the GPU closure kernels (BF16 tensor-core convolutions): the same
 three periodic 3x3x3 convolutions 4 -> 32 -> 32 -> 2 with GELU (tanh form), the same
 mean-squared-error loss and its exact gradient, in numpy float64.  The
 network has no counterpart in the reference; its definition is the one in

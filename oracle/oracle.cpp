@@ -1,11 +1,11 @@
 // oracle.cpp -- CPU FP64 restatement of the reference lattice hot path.
 //
-// TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU engine:
-// only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
-// it.  The engine never calls it and has no CPU fallback.
+// TEST INFRASTRUCTURE ONLY.  The GPU engine's results are compared with this
+// library's: only the tests, __graft_entry__.smoke() and bench.py's
+// CPU-baseline leg load it.  The engine never calls it and has no CPU fallback.
 //
 // Parity status: the reference is Fortran built against FFTW and MPI; neither
-// a Fortran compiler nor FFTW exists in this build environment, and the
+// a Fortran compiler nor FFTW exists in the development environment, and the
 // reference ships no tests, golden vectors or fixtures.  Parity against the
 // reference binary is therefore UNPINNED.  The restatement is pinned instead
 // by analytic known-answer tests (plane-wave Laplacian symbols, exact shell

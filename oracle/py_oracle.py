@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liblatoracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by the tests, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg as the checker.  The engine never imports it.
+bench.py's CPU-baseline leg, to compare the engine against.  The engine never imports it.
 Parity against the reference binary is unpinned (no Fortran compiler or FFTW
 exists to build the reference); the oracle is pinned by analytic known-answer
 tests and numpy.fft cross-checks instead.
