@@ -19,6 +19,15 @@ __device__ __forceinline__ float gelu_t(float z) {
   return 0.5f * z * (1.0f + tanh_hw(u));
 }
 
+// two values per instruction (packed FP32 arithmetic), same formula:
+// u = (sqrt(2/pi) z) (1 + 0.044715 z^2), gelu = (z/2) tanh(u) + z/2
+__device__ __forceinline__ float2 gelu_t2(float2 z) {
+  const float2 p = __ffma2_rn(__fmul2_rn(z, z), make_float2(0.044715f, 0.044715f), make_float2(1.0f, 1.0f));
+  const float2 u = __fmul2_rn(__fmul2_rn(z, make_float2(0.7978845608028654f, 0.7978845608028654f)), p);
+  const float2 hz = __fmul2_rn(z, make_float2(0.5f, 0.5f));
+  return __ffma2_rn(hz, make_float2(tanh_hw(u.x), tanh_hw(u.y)), hz);
+}
+
 __device__ __forceinline__ float gelu_t_d(float z) {
   const float z2 = z * z;
   const float t = tanh_hw(0.7978845608028654f * (z + 0.044715f * z2 * z));

@@ -113,7 +113,6 @@ __device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t phase) {
   return ok != 0;
 }
 
-__device__ __forceinline__ float gelu_f(float z) { return gelu_t(z); }
 __device__ __forceinline__ float gelu_df(float z) { return gelu_t_d(z); }
 
 // copies of halo plane z (periodic) of an item into ring slot `slot`
@@ -179,9 +178,11 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int zc,
 
   // epilogue geometry: warp w -> TMEM lanes 32 (w & 3) (sites), columns 16 (w >> 2) (channels)
   const int quarter = warp & 3, half = warp >> 2;
-  float bias[16];
+  float2 bias[8];
 #pragma unroll
-  for (int n = 0; n < 16; ++n) bias[n] = (EPI == EPI_GELU && a.bias && warp < 8) ? a.bias[16 * half + n] : 0.f;
+  for (int n = 0; n < 8; ++n)
+    bias[n] = (EPI == EPI_GELU && a.bias && warp < 8) ? make_float2(a.bias[16 * half + 2 * n], a.bias[16 * half + 2 * n + 1])
+                                                       : make_float2(0.f, 0.f);
 
   const int tiles_x = a.nx / XW, tiles_y = a.ny / IR, zchunks = (a.nz + zc - 1) / zc;
   const int64_t items_per = (int64_t)tiles_x * tiles_y * zchunks;
@@ -210,10 +211,9 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int zc,
         __align__(16) __nv_bfloat162 zz[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const float z0f = __uint_as_float(v[2 * j]) + bias[2 * j];
-          const float z1f = __uint_as_float(v[2 * j + 1]) + bias[2 * j + 1];
-          zz[j] = __floats2bfloat162_rn(z0f, z1f);
-          o[j] = __floats2bfloat162_rn(gelu_f(z0f), gelu_f(z1f));
+          const float2 zf = __fadd2_rn(make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), bias[j]);
+          zz[j] = __float22bfloat162_rn(zf);
+          o[j] = __float22bfloat162_rn(gelu_t2(zf));
         }
         if constexpr (STORE_Z) {
           uint4* zp = reinterpret_cast<uint4*>(a.zout + s * 32 + 16 * half);
