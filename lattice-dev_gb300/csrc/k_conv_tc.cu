@@ -113,7 +113,6 @@ __device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t phase) {
   return ok != 0;
 }
 
-__device__ __forceinline__ float gelu_df(float z) { return gelu_t_d(z); }
 
 // copies of halo plane z (periodic) of an item into ring slot `slot`
 template <int CA, int XW>
@@ -227,8 +226,9 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(ConvArgs a, int zc,
         reinterpret_cast<uint4*>(zz)[1] = zp[1];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const float g0 = gelu_df(__bfloat162float(zz[j].x)), g1 = gelu_df(__bfloat162float(zz[j].y));
-          o[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * g0, __uint_as_float(v[2 * j + 1]) * g1);
+          const float2 g = gelu_t_d2(__bfloat1622float2(zz[j]));
+          o[j] = __float22bfloat162_rn(
+              __fmul2_rn(make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), g));
         }
       }
       uint4* op = reinterpret_cast<uint4*>(a.out + s * 32 + 16 * half);
