@@ -382,13 +382,13 @@ int tc_xw(int nx, int ny) {
 }
 
 // z-planes per item: the fewest rounds of items over the SMs, counting the
-// item's pipeline fill (three planes before its first step) as three steps
+// item's pipeline fill (three plane copies, no epilogue) as one step
 int tc_zc(int64_t items_xy, int nz, int nsm) {
   int best = ZC_MAX;
   int64_t best_cost = -1;
   for (int zc = ZC_MAX; zc >= 4; zc /= 2) {
     const int64_t items = items_xy * ((nz + zc - 1) / zc);
-    const int64_t cost = ((items + nsm - 1) / nsm) * (std::min(zc, nz) + 3);
+    const int64_t cost = ((items + nsm - 1) / nsm) * (std::min(zc, nz) + 1);
     if (best_cost < 0 || cost < best_cost) best_cost = cost, best = zc;
   }
   return best;
