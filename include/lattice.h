@@ -11,6 +11,10 @@
  * Conventions (all entry points):
  *  - return an int status (LAT_OK == 0); nothing aborts the process;
  *    lat_last_error() gives a one-line message for the calling thread;
+ *  - LAT_ERR_NAN: a lattice reduction met NaN/Inf; lat_sync, lat_energies
+ *    and the calls that read the scalar block report it until a call that
+ *    replaces the fields (lat_upload, lat_gw_upload, lat_init_*,
+ *    lat_checkpoint_read) clears it;
  *  - a handle owns its device memory and one CUDA stream; handles are not
  *    thread-safe, distinct handles may be used from distinct threads;
  *  - the caller owns every host array; host field arrays use the Fortran

@@ -1159,11 +1159,18 @@ int lat_get_config(const lat_t* h, lat_config* cfg) {
   return LAT_OK;
 }
 
+// The NaN flag of the scalar block is sticky until the fields are replaced:
+// every call that uploads or draws a new state clears it (and drops
+// non-finite shifts carried over from the old state), so a handle that
+// reported LAT_ERR_NAN is usable again after a fresh upload.
+static int clear_nan_flag(lat_t* h) { return launch_state_reset(h->sc, h->stream); }
+
 int lat_upload(lat_t* h, const double* fld, int32_t fld_lo, int32_t fld_hi, const double* fldp, int32_t fldp_lo,
                int32_t fldp_hi) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   if (fld_lo < 0 || fld_hi < 0 || fldp_lo < 0 || fldp_hi < 0) return set_error(LAT_ERR_ARG, "negative padding");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)h->nf * h->N));
   if (fld) {
     const double* d = (fld_lo == 0 && fld_hi == 0) ? mapped_host(fld) : nullptr;
@@ -1433,6 +1440,7 @@ int lat_gw_upload(lat_t* h, const double* u, const double* pu) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   if (!h->cfg.gw) return set_error(LAT_ERR_STATE, "handle has no GW arrays");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)6 * h->N));
   if (u) {
     CK(cudaMemcpyAsync(h->stage, u, sizeof(double) * 6 * h->N, cudaMemcpyHostToDevice, h->stream));
@@ -1450,6 +1458,7 @@ int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0, const double* d
                     double amp, double kcut_frac) {
   if (!h || !fld0 || !dfld0 || !m2eff) return set_error(LAT_ERR_ARG, "null argument");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   const double twopi = 6.2831853071795864769252867665590;
   const double V = (h->nx * h->dx) * (h->ny * h->dx) * (h->nz * h->dx);
   const double Nd = (double)h->N;
@@ -1507,6 +1516,7 @@ int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0, const double* d
   if (!h || !fld0 || !dfld0 || !(mpl != 0.0)) return set_error(LAT_ERR_ARG, "null or zero argument");
   if (h->nx != h->ny || h->nx != h->nz) return set_error(LAT_ERR_UNSUPPORTED, "sample: cubic lattices");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   const int n = h->nx, os = 16, nos = n * os * os;
   const double twopi = 6.2831853071795864769252867665590;
   const double dk = twopi / (n * h->dx), dxos = h->dx / os, dkos = dk / (2.0 * os);
@@ -1587,6 +1597,7 @@ int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0, const double* d
 int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres, double radius, double width) {
   if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(width > 0)) return set_error(LAT_ERR_ARG, "bad bubble arguments");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)h->nf * h->N + 3 * 64));
   double* cen = h->stage + (size_t)h->nf * h->N;
   if (nbub > 0) CK(cudaMemcpyAsync(cen, centres, sizeof(double) * 3 * nbub, cudaMemcpyHostToDevice, h->stream));
@@ -1607,6 +1618,7 @@ int lat_init_bubbles_boosted(lat_t* h, int32_t nbub, const int32_t* centres, dou
   if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(r0 >= 0) || !(t0 >= 0))
     return set_error(LAT_ERR_ARG, "bad bubble arguments");
   ApiGuard g(h);
+  RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)std::max(h->nf, 2) * h->N + 3 * 64));
   double* phi = h->stage;
   double* pi = h->stage + h->N;

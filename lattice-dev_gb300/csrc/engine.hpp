@@ -179,6 +179,9 @@ struct KmulArgs {
 int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s);
 // a -= h * ap / 6 on the device (Hamiltonian_grav_kinetic)
 int launch_grav(DevScalars* sc, double h, cudaStream_t s);
+// New state in the handle: clear the NaN flag; non-finite carried shifts and
+// sums of the previous state become 0 (any finite shift is exact).
+int launch_state_reset(DevScalars* sc, cudaStream_t s);
 
 // ------------------------------------------------------- output kernels
 int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c,

@@ -319,6 +319,15 @@ __global__ void __launch_bounds__(256) kmul_kernel(KmulArgs a) {
 
 __global__ void grav_kernel(DevScalars* sc, double h) { sc->a = sc->a - h * sc->ap / 6.0; }
 
+__global__ void state_reset_kernel(DevScalars* sc) {
+  sc->err = 0u;
+  for (int i = 0; i < 4; ++i)
+    if (!isfinite(sc->mean[i])) sc->mean[i] = 0.0;
+  for (int i = 0; i < 2; ++i)
+    if (!isfinite(sc->zsh[i])) sc->zsh[i] = 0.0;
+  if (!isfinite(sc->ke_cur)) sc->ke_cur = 0.0;
+}
+
 // sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur
 __global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb) {
   KSum s;
@@ -421,6 +430,13 @@ int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int gri
   if (g_launch_counter) ++*g_launch_counter;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "momenta sum launch");
+}
+
+int launch_state_reset(DevScalars* sc, cudaStream_t s) {
+  state_reset_kernel<<<1, 1, 0, s>>>(sc);
+  if (g_launch_counter) ++*g_launch_counter;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LAT_OK : cuda_fail(e, "state reset launch");
 }
 
 int launch_grav(DevScalars* sc, double h, cudaStream_t s) {

@@ -54,6 +54,7 @@ struct Orc {
   double c[5] = {0, 0, 0, 0, 0};  // c0,c1,c2,c3,cc
   std::vector<double> fld, fldp;   // [f][z][y][x]
   std::vector<double> u, pu;       // GW [6][z][y][x]
+  std::vector<double> pu_next;     // GW kick scratch [6][z][y][x]
   std::vector<double> lap;         // scratch
   std::vector<cplx> Fk;            // scratch
   double a = 1.0, ap = 0.0;
@@ -204,23 +205,23 @@ void fields_kin(Orc& o, double dt) {
 // DEFROST Hamiltonian_metric_kin, Discrete/Bubble-Collisions/evolve.f90:497-500).
 void grav_kin(Orc& o, double dt) { o.a = o.a - dt * o.ap / 6.0; }
 
-// GW source d_i phi d_j phi with central differences, component c in the
-// order 11,22,33,12,13,23 (the reference's gw_source_* are empty stubs,
-// grav-waves/evolve-gw.f90:21-36).
+// GW source d_i phi d_j phi with central differences, all six components at
+// one site in the order 11,22,33,12,13,23 (the reference's gw_source_* are
+// empty stubs, grav-waves/evolve-gw.f90:21-36).  Each component sums the
+// fields in order, so the result does not depend on how many are computed.
 const int kGwI[6] = {0, 1, 2, 0, 0, 1};
 const int kGwJ[6] = {0, 1, 2, 1, 2, 2};
-double gw_source(const Orc& o, int x, int y, int z, int c) {
-  double s = 0;
+void gw_sources(const Orc& o, int x, int y, int z, double* src) {
   const double inv2dx = 1.0 / (2.0 * o.dx);
+  for (int cc = 0; cc < 6; ++cc) src[cc] = 0;
   for (int l = 0; l < o.nf; ++l) {
     const double* g = &o.fld[l * o.N];
     double d[3];
     d[0] = (g[idx3(wrap(x + 1, o.nx), y, z, o.nx, o.ny)] - g[idx3(wrap(x - 1, o.nx), y, z, o.nx, o.ny)]) * inv2dx;
     d[1] = (g[idx3(x, wrap(y + 1, o.ny), z, o.nx, o.ny)] - g[idx3(x, wrap(y - 1, o.ny), z, o.nx, o.ny)]) * inv2dx;
     d[2] = (g[idx3(x, y, wrap(z + 1, o.nz), o.nx, o.ny)] - g[idx3(x, y, wrap(z - 1, o.nz), o.nx, o.ny)]) * inv2dx;
-    s += d[kGwI[c]] * d[kGwJ[c]];
+    for (int cc = 0; cc < 6; ++cc) src[cc] += d[kGwI[cc]] * d[kGwJ[cc]];
   }
-  return s;
 }
 
 // Hamiltonian_fields_grad_pot: spectral hamiltonian_conformal.f90:128-174
@@ -236,16 +237,20 @@ void fields_grad_pot(Orc& o, double dt) {
   if (o.cfg.gw) {
     const double elap = 1.0 / (o.dx * o.dx) / o.c[4];
     const double kap = o.cfg.gw_coupling;
-    std::vector<double> newpu(6 * o.N);
+    std::vector<double>& newpu = o.pu_next;
+    newpu.resize(6 * o.N);
 #pragma omp parallel for schedule(static)
     for (int z = 0; z < o.nz; ++z)
       for (int y = 0; y < o.ny; ++y)
-        for (int x = 0; x < o.nx; ++x)
+        for (int x = 0; x < o.nx; ++x) {
+          const int64_t s = idx3(x, y, z, o.nx, o.ny);
+          double src[6];
+          gw_sources(o, x, y, z, src);
           for (int cc = 0; cc < 6; ++cc) {
-            int64_t s = idx3(x, y, z, o.nx, o.ny);
             double lu = stencil_sum(o, &o.u[cc * o.N], x, y, z) * elap;
-            newpu[cc * o.N + s] = o.pu[cc * o.N + s] + dt * (lu + kap * gw_source(o, x, y, z, cc));
+            newpu[cc * o.N + s] = o.pu[cc * o.N + s] + dt * (lu + kap * src[cc]);
           }
+        }
     o.pu.swap(newpu);
   }
   for (int l = 0; l < o.nf; ++l) {

@@ -34,6 +34,8 @@ def test_mode_counts_golden(orc):
     g = np.load(GOLD / "mode_counts.npz")
     for key in [k for k in g.files if k.startswith("W_")]:
         nx, ny, nz = map(int, key.split("_")[1:])
+        if nx * ny * nz > 256 ** 3:
+            continue  # 512^3: checked on the GPU machine (tests/test_gpu_benchsize.py), engine and oracle
         c = L.make_config((nx, ny, nz), nfld=1, length=1.0)
         o = orc.Oracle(c)
         assert o.nbins() == int(g[f"ns_{nx}_{ny}_{nz}"])
