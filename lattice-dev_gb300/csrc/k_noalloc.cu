@@ -119,6 +119,9 @@ __global__ void __launch_bounds__(256) na_spec_kernel(NaArgs a) {
   if (threadIdx.x == 0) *counter = 0u;
 }
 
+// Device address of g_na_scratch per device ordinal, looked up by the first
+// call on that device and kept for the life of the process (a device reset
+// after that call is not supported).
 std::mutex g_na_mu;
 double* g_na_addr[64] = {};
 
@@ -153,7 +156,11 @@ extern "C" int lat_spectrum_noalloc(const void* Fk_dev, int32_t nx, int32_t ny, 
     scratch = g_na_addr[dev];
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // the arrival counter must start at zero
+  // the arrival counter must start at zero.  The last block of every
+  // completed launch resets it, but a launch that was aborted (a failed
+  // launch, a lost context that was recovered) can leave it set, and a stale
+  // count would make a block other than the last one sum the partials: keep
+  // this memset.
   e = cudaMemsetAsync(scratch, 0, kNaHeader * sizeof(double), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   NaArgs a{};

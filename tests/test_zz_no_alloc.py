@@ -6,8 +6,11 @@ not allocate): it takes a half spectrum and an output buffer already on the
 device and keeps its scratch in a fixed static device array.  This test gives
 it the half spectrum of a lattice field (made here with torch, since the test
 itself may allocate), calls it twice in a row, and checks both results against
-lat_spectrum on the same field.  It lives in its own file so that it runs
-after every other test.
+lat_spectrum on the same field; around the second call the device's free
+memory must not change (a cudaMalloc, or a library routine that allocates a
+workspace, would show up there).  It lives in its own file, collected last, so
+that a run stopping at the first failure has already run every other test
+when this one fails; it also passes alone in a fresh process.
 """
 from __future__ import annotations
 
@@ -45,8 +48,12 @@ def test_spectrum_noalloc_matches_lat_spectrum(engine, prec, tol, mode):
     stored = f if prec == 0 else f.astype(np.float32)  # the FP32 lattice transforms its FP32 field
     F = torch.fft.rfftn(torch.from_numpy(np.ascontiguousarray(stored)).to("cuda", dtype)).contiguous()
     out = torch.full((2 * nbins,), -1.0, dtype=torch.float64, device="cuda")
-    for _ in range(2):  # two calls in a row share the static scratch
+    for call in range(2):  # two calls in a row share the static scratch
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         S, W = _noalloc(engine, F, shape, prec, mode, nbins, out, torch)
+        if call == 1:  # the first call may load the module's device code; the second allocates nothing
+            assert torch.cuda.mem_get_info()[0] == free0
         assert np.max(np.abs(S - S_ref)) <= tol * np.max(np.abs(S_ref))
         if mode == 1:
             assert np.array_equal(W, W_ref)
