@@ -218,7 +218,10 @@ int lat_spectrum_3d(int32_t n1, int32_t n2, int32_t n3, const double* f,
  * library keeps until exit; nbins above 512 is rejected with LAT_ERR_ARG.
  * All calls share that scratch: calls that overlap on the GPU race, so order
  * them.  The first call on a device looks up the scratch's device address
- * (with that device current); make it before any stream capture. */
+ * (with that device current) and keeps it for the life of the process; make
+ * it before any stream capture.  A device reset (cudaDeviceReset, or a
+ * destroyed and recreated primary context) after that first call is not
+ * supported: the kept address would no longer be valid. */
 int lat_spectrum_noalloc(const void* Fk_dev, int32_t nx, int32_t ny, int32_t nz,
                          int32_t precision, int32_t mode, int32_t nbins,
                          double* out_dev, void* stream);

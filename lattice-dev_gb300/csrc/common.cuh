@@ -34,7 +34,7 @@ struct DevScalars {
   double mean[4];  // lattice means of the fields (spectral shift of the separable passes)
   double zsh[2];   // shift the zs array of the last streamed kick was taken with (k_sep_stream.cuh)
   double ke_cur;   // sum pi^2 of the current momenta, kept by the streamed passes
-  unsigned int err;  // bit 0: NaN/Inf met in a reduction
+  unsigned int err;  // bit 0: NaN/Inf met in a reduction; bit 1: a bounded device wait gave up
   unsigned int pad[3];
 };
 

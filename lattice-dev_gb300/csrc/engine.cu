@@ -412,6 +412,52 @@ int exec_plain(lat_s* h, const std::vector<Op>& ops) {
   return LAT_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+}  // namespace
+
+int lat::encode_stream_tmaps(SepArgs& a, int axis, int lines, int n) {
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return set_error(LAT_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+  const cuuint64_t nx = (cuuint64_t)a.nx, ny = (cuuint64_t)a.ny, nz = (cuuint64_t)a.nz;
+  const cuuint32_t L = (cuuint32_t)lines, N = (cuuint32_t)n;
+  // zs: both fields interleaved, float2 per site, addressed as floats
+  const cuuint64_t zdim[3] = {2 * nx, ny, nz};
+  const cuuint64_t zstr[2] = {2 * nx * 4, 2 * nx * ny * 4};
+  const cuuint32_t zbox[3] = {2 * L, axis == 1 ? N : 1u, axis == 2 ? N : 1u};
+  const cuuint32_t one[4] = {1, 1, 1, 1};
+  CUresult r = enc(&a.tm_zs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(a.lap), zdim, zstr, zbox, one,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(LAT_ERR_CUDA, "tensor map of zs: error " + std::to_string((int)r));
+  // momenta of the two fields, N sites apart
+  const cuuint64_t pdim[4] = {nx, ny, nz, 2};
+  const cuuint64_t pstr[3] = {nx * 4, nx * ny * 4, nx * ny * nz * 4};
+  const cuuint32_t pbox[4] = {L, axis == 1 ? N : 1u, axis == 2 ? N : 1u, 2};
+  r = enc(&a.tm_pi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.pi_out, pdim, pstr, pbox, one,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(LAT_ERR_CUDA, "tensor map of the momenta: error " + std::to_string((int)r));
+  return LAT_OK;
+}
+
+namespace {
+
 // One separable spectral pass (k_sep.cuh) along `axis`.
 int sep_pass(lat_s* h, int axis, double hk, double hg, double hd, int* grid_out = nullptr) {
   static const int kcls[3] = {LAT_K_SEP_X, LAT_K_SEP_Y, LAT_K_SEP_Z};
@@ -455,6 +501,10 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd, int* grid_out 
   a.stream = h->sep_stream ? 1 : 0;
   a.runs = 0;                // the two fields of this lattice form one pair
   a.pair_lines = a.nlines;
+  if (h->sep_stream && axis > 0) {  // passes Y and Z move their tiles by TMA
+    const int lines = n == 128 ? sep_stream_lines_128(axis) : sep_stream_lines_256(axis);
+    RET(encode_stream_tmaps(a, axis, lines, n));
+  }
   int st;
   switch (n) {
     case 16: st = launch_sep_16(a, h->prec, axis, h->stream); break;
@@ -751,6 +801,7 @@ int compute_energies(lat_s* h, double* out, double ball_r2 = 0.0, double* ball =
   }
   DevScalars s;
   RET(read_scalars(h, &s));
+  if (s.err & 2u) return set_error(LAT_ERR_TIMEOUT, "a tensor copy of a streamed pass was not completed in time");
   if (s.err & 1u) return set_error(LAT_ERR_NAN, "NaN/Inf in a lattice reduction");
   const bool conf = conformal(h);
   const double a = conf ? s.a : 1.0;
@@ -1295,6 +1346,7 @@ int lat_sync(lat_t* h) {
   CK(cudaStreamSynchronize(h->stream));
   unsigned int err = 0;
   CK(cudaMemcpy(&err, &h->sc->err, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  if (err & 2u) return set_error(LAT_ERR_TIMEOUT, "a tensor copy of a streamed pass was not completed in time");
   if (err & 1u) return set_error(LAT_ERR_NAN, "NaN/Inf in a lattice reduction");
   if (h->cl_net) {
     int cerr = 0;

@@ -1,6 +1,7 @@
 // engine.hpp -- host-side structures of the GB300 lattice engine and the
 // launchers each kernel translation unit exports.
 #pragma once
+#include <cuda.h>  // CUtensorMap (tensor-memory-access descriptors; encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -14,6 +15,26 @@ namespace lat {
 // Set the thread's error message and return `code`.
 int set_error(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
+
+// Launch `k` as a programmatic dependent of the previous kernel in stream s
+// (programmatic stream serialization): it may start while that kernel
+// drains and must order its reads of the predecessor's outputs with
+// griddepcontrol.wait.  Stream capture records the dependency as a
+// programmatic graph edge.
+template <typename K, typename... Args>
+cudaError_t launch_pdl(K k, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const Args&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // ------------------------------------------------------------ FD passes
 // One tiled stencil pass: kick (and optionally drift) of the fields and,
@@ -102,7 +123,16 @@ struct SepArgs {
   int* grid_out;            // host: receives the grid of a streamed pass (or null)
   DevScalars* sc;
   RedBuf rb;
+  // streamed passes Y and Z of two fields: tensor maps of zs (float, dims
+  // {2 nx, ny, nz}, box {2 LINES, N, 1} for Y and {2 LINES, 1, N} for Z) and
+  // of the momenta (dims {nx, ny, nz, 2 fields}, box {LINES, N, 1, 2} or
+  // {LINES, 1, N, 2}); a tile is one TMA load of each and one TMA store
+  CUtensorMap tm_zs;
+  CUtensorMap tm_pi;
 };
+// Encode the two tensor maps of a streamed pass along `axis` (1 or 2) with
+// `lines` x-columns per tile and line length n.
+int encode_stream_tmaps(SepArgs& a, int axis, int lines, int n);
 int launch_sep_16(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_32(const SepArgs& a, int precision, int axis, cudaStream_t s);
 int launch_sep_64(const SepArgs& a, int precision, int axis, cudaStream_t s);

@@ -25,15 +25,28 @@
 // each run's phi at site 0 as it was after the previous kick.
 //
 // Blocks are persistent.  A block reads the inputs of its tile from shared
-// memory into registers, refills the slot with the next tile's inputs by
-// cp.async at once, and runs the line transforms in a separate scratch, so the
-// next tile's HBM reads are in flight during the transforms.  Pass X: 128
-// threads per block; every warp stages and transforms its own lines with warp
-// barriers only.  Passes Y, Z: 32 x-columns per block (128-byte rows of
+// memory into registers, refills the slot with the next tile's inputs at
+// once, and runs the line transforms in a separate scratch, so the next
+// tile's HBM reads are in flight during the transforms.  Pass X: 128 threads
+// per block; every warp stages (cp.async) and transforms its own lines with
+// warp barriers only.  Passes Y, Z: 32 x-columns per block (128-byte rows of
 // momenta: at 16 columns the strided 64-byte rows ran both passes 4-6%
 // slower), with a second slot for the momenta, which are needed only after
-// the transform.  Every update of a tile is written by the block that read it,
-// so the passes also run in place.
+// the transform; for two fields each slot is filled by one TMA tensor copy
+// (zs: a 3D box, the momenta of both fields: one 4D box) issued by one
+// thread and counted on an mbarrier, for pairs of runs by cp.async.  Every
+// update of a tile is written by the block that read it, so the passes also
+// run in place.
+//
+// The two-field chain X, Y, Z, finalize is launched with programmatic
+// dependent launch: each pass starts while its predecessor drains and waits
+// (griddepcontrol.wait) only before reading what the predecessor writes.
+// Pass X stages the phi and c of its first tile early (last written by the
+// previous pass X), pass Z its first zs tile and that tile's transform (zs
+// comes from pass X; pass Y writes only the momenta).  The FP64 coefficient
+// chain of a kick is evaluated once per warp (X) or per block (Y, Z), not
+// per thread: at GB300's FP64 rate the per-thread chain had cost pass Z
+// 13 us of its 92 us at 256^3.
 #pragma once
 #include "k_sep.cuh"
 
@@ -166,6 +179,55 @@ struct STile {
   static_assert(RS % 4 == 0 && N % 4 == 0, "staged rows must hold whole 16-byte copies");
 };
 
+
+// ------------------------------------------------ tensor memory access (TMA)
+// One thread issues a tile copy described by a tensor map; completion is
+// counted in bytes on an mbarrier that every consumer waits on.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of `parity`: false if it did not complete
+// within the limit (the caller records the timeout and leaves).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < (1u << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+// order this thread's generic-proxy shared-memory accesses before later
+// async-proxy (TMA) accesses of the same memory
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
 // First-line geometry of a tile: the pair it belongs to and the offset of
 // line A's first site.  Two fields: one pair (pair_lines = nlines).
 template <int AXIS>
@@ -228,7 +290,8 @@ __device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t
 
 // Pass X staging by one warp: the rows of its own 32/P lines of tile `tile`
 // (6 arrays: [line A, B][phi, c, pi]), so the warp waits only for its copies.
-template <int N>
+// WHICH: 3 = all six arrays, 1 = phi and c only, 2 = pi only.
+template <int N, int WHICH = 3>
 __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64_t tile, int warp, int lane) {
   using T = STile<0, N>;
   constexpr int LPW = 32 / T::P, CPR = N / 4;  // lines per warp, 16-byte chunks per row
@@ -239,6 +302,7 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
 #pragma unroll
   for (int arr = 0; arr < 6; ++arr) {
     const int f = arr / 3, k = arr % 3;
+    if (!((k == 2 ? 2 : 1) & WHICH)) continue;
     const void* sp = k == 0 ? a.phi : (k == 1 ? a.phic : a.pi);
     const float* src = static_cast<const float*>(sp) + f * Ns + r0;
 #pragma unroll
@@ -247,6 +311,36 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
       cp16(d0 + arr * T::ARR + r * T::RS + c * 4, src + (int64_t)r * a.nx + c * 4);
     }
   }
+}
+
+// The kick's FP32 coefficients from the scalar block's pre-kick state
+// (hamiltonian_conformal.f90:86-174): cd = hd/a0^2, ck = hk a1^2,
+// cv = hk a1^4 with a1 after the drift's ysclp update and the gravity half
+// step.  GB300's FP64 rate makes the chain cost microseconds when every
+// thread of a block evaluates it, so one thread does: kick_coefs() into
+// shared memory (thread 0, read after the next block barrier), or
+// kick_coefs_warp() in lane 0 of every warp, broadcast by shuffle.
+__device__ __forceinline__ void kick_coefs_eval(const SepArgs& a, float (&c)[3]) {
+  const DevScalars* sc = a.sc;
+  const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
+  const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
+  const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
+  c[0] = (float)(a.hd / (a0 * a0));
+  c[1] = (float)(a.hk * a1 * a1);
+  c[2] = (float)(a.hk * a1 * a1 * a1 * a1);
+}
+__device__ __forceinline__ void kick_coefs(const SepArgs& a, float* coef, int tid) {
+  if (tid != 0) return;
+  float c[3];
+  kick_coefs_eval(a, c);
+  coef[0] = c[0];
+  coef[1] = c[1];
+  coef[2] = c[2];
+}
+__device__ __forceinline__ void kick_coefs_warp(const SepArgs& a, float (&c)[3], int lane) {
+  if (lane == 0) kick_coefs_eval(a, c);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) c[i] = __shfl_sync(0xffffffffu, c[i], 0);
 }
 
 // Pass X: drift, zs and the x part of the kick.
@@ -265,9 +359,23 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   const int tid = threadIdx.x, t = tid % P, li = tid / P, warp = tid / 32, lane = tid % 32;
   const int64_t ntiles = a.nlines / LINES;
   const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (my > 0) stage_rows_x<N>(a, es, blockIdx.x, warp, lane);
-  cp_commit();
-  build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+  if constexpr (!RUNS) {
+    // launched as a programmatic dependent of the previous kick's finalize:
+    // phi and c were last written by the previous pass X, so the first
+    // tile's phi and c are staged while the predecessor drains; the momenta
+    // (previous pass Z) and the scalar block (finalize) only after the wait
+    if (my > 0) stage_rows_x<N, 1>(a, es, blockIdx.x, warp, lane);
+    cp_commit();
+    build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+    pdl_wait();
+    pdl_trigger();
+    if (my > 0) stage_rows_x<N, 2>(a, es, blockIdx.x, warp, lane);
+    cp_commit();
+  } else {
+    if (my > 0) stage_rows_x<N>(a, es, blockIdx.x, warp, lane);
+    cp_commit();
+    build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+  }
   __syncthreads();  // tables; from here on every warp runs its own lines
 
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
@@ -285,12 +393,11 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   }
   const bool drift = a.hd != 0.0;
   float cd = (float)a.hd, ck = (float)a.hk;
-  if (CONF) {
-    const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
-    const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
-    const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
-    cd = (float)(a.hd / (a0 * a0));
-    ck = (float)(a.hk * a1 * a1);
+  if (CONF) {  // the scalar block is read after the wait above
+    float c[3];
+    kick_coefs_warp(a, c, lane);
+    cd = c[0];
+    ck = c[1];
   }
   KSum ge, pe, mA, mB;
   // pairs of runs: each run's shift is its phi at site 0 after the previous
@@ -517,14 +624,207 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   }
 }
 
+
+// Passes Y and Z of two fields with TMA: a tile's zs rows (64 KB at 256
+// points) and both fields' momentum rows (one 4D box) arrive by one tensor
+// copy each, counted on an mbarrier per slot, issued by one thread; the
+// updated momenta are stored from registers (128-byte rows per warp), so the
+// momentum slot takes the next tile as soon as every thread has read it (a
+// tensor store from the slot would hold the next copy until the store had
+// read the slot, and every warp waited for that at the next barrier).  Launched as
+// programmatic dependents: pass Y (after pass X, which writes zs and the
+// momenta) waits before its first copy; pass Z (after pass Y, which writes
+// only the momenta) loads and transforms its first zs tile while Y drains.
+// A bounded mbarrier wait that gives up sets bit 1 of the scalar block's
+// error word (reported as LAT_ERR_TIMEOUT) and the block leaves.
+// MODEL >= 0: the potential fixed at compile time (the model switch folds
+// away in pass Z); -1: read from the arguments.
+template <int AXIS, int N, bool CONF, int MODEL = -1>
+__global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
+    sep_stream_yz_tma(const __grid_constant__ SepArgs a) {
+  using T = STile<AXIS, N>;
+  constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
+  constexpr uint32_t ZS_BYTES = 2u * LINES * N * 4u;  // box {2 LINES, N} floats
+  constexpr uint32_t PI_BYTES = 2u * LINES * N * 4u;  // box {LINES, N, 2 fields} floats
+  static_assert(T::E_OFF == 0 && (T::L_OFF * 4) % 128 == 0, "TMA slots must be 128-byte aligned");
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t bar[2];  // [0]: zs slot, [1]: momentum slot
+  __shared__ float coef[3];
+  // the dynamic region starts after the static variables: the slots begin at
+  // its first 128-byte boundary (the launch adds 128 bytes)
+  unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+  float* sm = reinterpret_cast<float*>(base);
+  float* es = sm + T::E_OFF;
+  float* ls = sm + T::L_OFF;
+  float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
+  float2* tf = reinterpret_cast<float2*>(sm + T::TF_OFF);
+  float2* ti = reinterpret_cast<float2*>(sm + T::TI_OFF);
+  float* fk = sm + T::FK_OFF;
+  const int tid = threadIdx.x, t = tid / LINES, li = tid % LINES;
+  const int64_t ntiles = a.nlines / LINES;
+  const int my = ntiles > (int64_t)blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  // tile -> (first x-column, plane index along the other axis): the lines
+  // of pass Y are (x, z), those of pass Z (x, y)
+  auto coords = [&](int tile, int& x0, int& o) {
+    const uint32_t r = (uint32_t)tile * LINES, nx = (uint32_t)a.nx;
+    o = (int)(r / nx);
+    x0 = (int)(r - (uint32_t)o * nx);
+  };
+  auto load_zs = [&](int tile) {
+    int x0, o;
+    coords(tile, x0, o);
+    mbar_expect_tx(&bar[0], ZS_BYTES);
+    if (AXIS == 1) tma_load_3d(es, &a.tm_zs, &bar[0], 2 * x0, 0, o);
+    else tma_load_3d(es, &a.tm_zs, &bar[0], 2 * x0, o, 0);
+  };
+  auto load_pi = [&](int tile) {
+    int x0, o;
+    coords(tile, x0, o);
+    mbar_expect_tx(&bar[1], PI_BYTES);
+    if (AXIS == 1) tma_load_4d(ls, &a.tm_pi, &bar[1], x0, 0, o, 0);
+    else tma_load_4d(ls, &a.tm_pi, &bar[1], x0, o, 0, 0);
+  };
+  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
+  const int64_t st = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
+  float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
+
+  if (smem_u32(base) & 127u) {  // tensor copies need 128-byte aligned slots: refuse, never misaddress
+    if (tid == 0) atomicOr(&a.sc->err, 2u);
+    return;
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if constexpr (AXIS == 1) {
+    build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+    pdl_wait();
+    pdl_trigger();
+    if (tid == 0 && my > 0) {
+      load_zs(blockIdx.x);
+      load_pi(blockIdx.x);
+    }
+  } else {
+    if (tid == 0 && my > 0) load_zs(blockIdx.x);  // zs was written two kernels back (pass X)
+    build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
+  }
+  if (CONF) kick_coefs(a, coef, tid);  // read after the first barrier of the tile loop
+
+  const DevScalars* sc = a.sc;  // written by the finalize three kernels back
+  float zshA = 0.f, zshB = 0.f;
+  if (AXIS == 2) {
+    zshA = (float)__ldcg(&sc->mean[0]);
+    zshB = (float)__ldcg(&sc->mean[1]);
+  }
+  float ck = (float)a.hk, cv = (float)a.hk;  // static background; expanding: coef[] after the first barrier
+  ModelP mp = a.model;
+  if constexpr (MODEL >= 0) mp.model = MODEL;
+  KSum ge, ke;
+  int fail = 0;
+  for (int j = 0; j < my; ++j) {
+    const int tile = (int)blockIdx.x + j * (int)gridDim.x;
+    const uint32_t ph = (uint32_t)(j & 1);
+    fail = !mbar_wait(&bar[0], ph);
+    if (__syncthreads_or(fail)) break;
+    if (CONF && j == 0) {
+      ck = coef[1];
+      cv = coef[2];
+    }
+    float vr[Q], vi[Q];
+    float hA[AXIS == 2 ? Q : 1], hB[AXIS == 2 ? Q : 1];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int pos = t + P * q;
+      const float2 z = reinterpret_cast<const float2*>(es)[pos * T::RS + li];
+      vr[q] = z.x;
+      vi[q] = z.y;
+      if constexpr (AXIS == 2) {
+        hA[q] = vr[q] + zshA;  // phi - c
+        hB[q] = vi[q] + zshB;
+      }
+    }
+    __syncthreads();  // every thread has its zs: the slot takes the next tile
+    if (tid == 0 && j + 1 < my) {
+      fence_proxy_async();
+      load_zs(tile + (int)gridDim.x);
+    }
+    d2_line_tab<N, false, CONF>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
+    if (AXIS == 2 && j == 0) {  // pass Y has completed: its momenta may be read
+      pdl_wait();
+      pdl_trigger();
+      if (tid == 0) load_pi(tile);
+    }
+    fail = !mbar_wait(&bar[1], ph);
+    if (__syncthreads_or(fail)) break;
+    int x0, o;
+    coords(tile, x0, o);
+    const int64_t offA = (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0 + li, offB = Nsite + offA;
+    float kes[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int pos = t + P * q;
+      const float* pa = ls + pos * T::RS + li;
+      float pA = pa[0], pB = pa[T::ARR];
+      if constexpr (AXIS == 1) {
+        pA = pA + ck * vr[q];
+        pB = pB + ck * vi[q];
+      } else {
+        float ff[2] = {hA[q], hB[q]}, dv[2];
+        model_dv<float, 2>(mp, ff, dv);
+        pA = pA + (ck * vr[q] - cv * dv[0]);
+        pB = pB + (ck * vi[q] - cv * dv[1]);
+        if (CONF) kes[q % 4] += pA * pA + pB * pB;
+      }
+      pi_o[offA + (int64_t)pos * st] = pA;
+      pi_o[offB + (int64_t)pos * st] = pB;
+    }
+    if (AXIS == 2 && CONF) ke.add((kes[0] + kes[1]) + (kes[2] + kes[3]));
+    __syncthreads();  // every thread has read its momenta: the slot takes the next tile
+    if (tid == 0 && j + 1 < my) {
+      fence_proxy_async();
+      load_pi(tile + (int)gridDim.x);
+    }
+  }
+  if (fail) {
+    // a copy never completed: record it, give the copies in flight a
+    // bounded wait, and leave without partial sums
+    if (tid == 0) {
+      atomicOr(&a.sc->err, 2u);
+      mbar_wait(&bar[0], 0u);
+      mbar_wait(&bar[0], 1u);
+      mbar_wait(&bar[1], 0u);
+      mbar_wait(&bar[1], 1u);
+    }
+    return;
+  }
+  if constexpr (!CONF) return;
+  if constexpr (AXIS == 1) {
+    const FF vals[1] = {ge.red()};
+    block_partials<1>(vals, a.rb.partials + SEP_PART_Y);
+  } else {
+    const FF vals[2] = {ge.red(), ke.red()};
+    block_partials<2>(vals, a.rb.partials + SEP_PART_Z);
+  }
+}
+
+// pdl: launch as a programmatic dependent of the previous kernel in the
+// stream (the two-field passes, which order their reads by pdl_wait)
 template <typename K>
-int stream_launch(K k, int smem, int threads, int minb, int64_t ntiles, const SepArgs& a, cudaStream_t s) {
+int stream_launch(K k, int smem, int threads, int minb, int64_t ntiles, const SepArgs& a, cudaStream_t s,
+                  bool pdl = false) {
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return cuda_fail(e, "streamed separable pass smem attribute");
   const int64_t cap = (int64_t)minb * a.nsm;
   const int grid = (int)(ntiles < cap ? ntiles : cap);
   if (a.grid_out) *a.grid_out = grid;  // host side: the blocks whose partials the finalize sums
-  k<<<grid, threads, smem, s>>>(a);
+  if (pdl) {
+    e = launch_pdl(k, dim3(grid), dim3(threads), (size_t)smem, s, a);
+    if (e != cudaSuccess) return cuda_fail(e, "streamed separable pass launch");
+  } else {
+    k<<<grid, threads, smem, s>>>(a);
+  }
   if (g_launch_counter) ++*g_launch_counter;
   e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "streamed separable pass launch");
@@ -548,25 +848,38 @@ int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
   const int64_t ntiles = a.nlines / lines;
   // an expanding background (two fields only) adds the lattice sums of the
   // Friedmann update; a static one needs none of them
+  constexpr bool PDL = !RUNS;  // the two-field chain X, Y, Z, finalize
   if constexpr (!RUNS) {
     if (a.conf) {
       switch (axis) {
         case 0: return stream_launch(sep_stream_x<N, false, true>, STile<0, N>::SMEM, STile<0, N>::THREADS,
-                                     STile<0, N>::MINB, ntiles, a, s);
-        case 1: return stream_launch(sep_stream_yz<1, N, false, true>, STile<1, N>::SMEM, STile<1, N>::THREADS,
-                                     STile<1, N>::MINB, ntiles, a, s);
-        default: return stream_launch(sep_stream_yz<2, N, false, true>, STile<2, N>::SMEM, STile<2, N>::THREADS,
-                                      STile<2, N>::MINB, ntiles, a, s);
+                                     STile<0, N>::MINB, ntiles, a, s, PDL);
+        case 1: return stream_launch(sep_stream_yz_tma<1, N, true>, STile<1, N>::SMEM + 128, STile<1, N>::THREADS,
+                                     STile<1, N>::MINB, ntiles, a, s, PDL);
+        default:
+          if (a.model.model == LAT_MODEL_PHI4_G2)
+            return stream_launch(sep_stream_yz_tma<2, N, true, LAT_MODEL_PHI4_G2>, STile<2, N>::SMEM + 128,
+                                 STile<2, N>::THREADS, STile<2, N>::MINB, ntiles, a, s, PDL);
+          return stream_launch(sep_stream_yz_tma<2, N, true>, STile<2, N>::SMEM + 128, STile<2, N>::THREADS,
+                               STile<2, N>::MINB, ntiles, a, s, PDL);
       }
     }
   }
+  if constexpr (!RUNS) {
+    if (axis == 1)
+      return stream_launch(sep_stream_yz_tma<1, N, false>, STile<1, N>::SMEM + 128, STile<1, N>::THREADS,
+                           STile<1, N>::MINB, ntiles, a, s, PDL);
+    if (axis == 2)
+      return stream_launch(sep_stream_yz_tma<2, N, false>, STile<2, N>::SMEM + 128, STile<2, N>::THREADS,
+                           STile<2, N>::MINB, ntiles, a, s, PDL);
+  }
   switch (axis) {
     case 0: return stream_launch(sep_stream_x<N, RUNS, false>, STile<0, N>::SMEM, STile<0, N>::THREADS,
-                                 STile<0, N>::MINB, ntiles, a, s);
+                                 STile<0, N>::MINB, ntiles, a, s, PDL);
     case 1: return stream_launch(sep_stream_yz<1, N, RUNS, false>, STile<1, N>::SMEM, STile<1, N>::THREADS,
-                                 STile<1, N>::MINB, ntiles, a, s);
+                                 STile<1, N>::MINB, ntiles, a, s, PDL);
     default: return stream_launch(sep_stream_yz<2, N, RUNS, false>, STile<2, N>::SMEM, STile<2, N>::THREADS,
-                                  STile<2, N>::MINB, ntiles, a, s);
+                                  STile<2, N>::MINB, ntiles, a, s, PDL);
   }
 }
 

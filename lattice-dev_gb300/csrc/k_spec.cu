@@ -330,6 +330,10 @@ __global__ void state_reset_kernel(DevScalars* sc) {
 
 // sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur
 __global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb) {
+  // first kernel of a streamed call, launched with programmatic serialization
+  // (the wait returns at once when nothing precedes it programmatically)
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   KSum s;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
     const float4 v = __ldcs(pi + i);
@@ -371,6 +375,9 @@ __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
   // flight at once; the order of every sum is fixed
   __shared__ double tot[8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // a programmatic dependent of pass Z: its partials are read after the wait
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   if (wid < 7) {
     const int p = wid < 4 ? 0 : (wid == 4 ? 1 : 2);
     const int nv = p == 0 ? 4 : (p == 1 ? 1 : 2), i = p == 0 ? wid : (p == 1 ? 0 : wid - 5);
@@ -418,17 +425,19 @@ __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
 }
 
 int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s) {
-  sep_finalize_kernel<<<1, 256, 0, s>>>(f);
+  cudaError_t e = launch_pdl(sep_finalize_kernel, dim3(1), dim3(256), 0, s, f);
+  if (e != cudaSuccess) return cuda_fail(e, "separable finalize launch");
   if (g_launch_counter) ++*g_launch_counter;
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "separable finalize launch");
 }
 
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s) {
   if (n % 4) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
-  pi2_kernel<<<grid, 256, 0, s>>>(static_cast<const float4*>(pi), n / 4, sc, rb);
+  cudaError_t e = launch_pdl(pi2_kernel, dim3(grid), dim3(256), 0, s, static_cast<const float4*>(pi), n / 4, sc, rb);
+  if (e != cudaSuccess) return cuda_fail(e, "momenta sum launch");
   if (g_launch_counter) ++*g_launch_counter;
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "momenta sum launch");
 }
 
