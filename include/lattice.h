@@ -424,6 +424,46 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units);
  * kick misses) into out_dev, in the variables `units` selects. */
 int lat_coarsen(lat_t* fine, int32_t nc, int32_t units, float* out_dev);
 
+/* ------------------------------------------------------ z-slab decomposition */
+/* A handle for the z-planes [z0, z1) of a global periodic lattice, one per
+ * rank of a decomposed run: the MPI slab split of the reference, where each
+ * rank owns a range of planes, exchanges one ghost plane with each z
+ * neighbour before every FD kick and all-reduces the lattice sums of the
+ * Friedmann update (Pseudospec/mpi_dev/hamiltonian_minkowski.f90:297-342,
+ * hamiltonian_conformal.f90:112-114,198-201; the DEFROST tree's wrap_field
+ * for z, Discrete/Bubble-Collisions/scafld.f90:120-192).  Finite-difference
+ * stencils only (7 or 27 points, GW strains included); the spectral
+ * Laplacian's distributed transform is not built (lat_slab_create refuses
+ * it with LAT_ERR_UNSUPPORTED).  Field arrays of lat_upload/lat_download and
+ * lat_gw_upload/lat_gw_download on a slab hold its nz_loc = z1 - z0 interior
+ * planes, unpadded.  The caller moves the data between ranks (MPI, NCCL,
+ * torch.distributed): two hooks are called from inside lat_symp, lat_split,
+ * lat_o2step, lat_energies and lat_calc_metric, which then run without CUDA
+ * graphs:
+ *   halo(user, h): fill both ghost planes of h, e.g. lat_slab_halo packs of
+ *     the boundary planes sent to the z neighbours and unpacks of what they
+ *     sent; called before every kick and every energy reduction;
+ *   sum(user, v, n): replace the n doubles of v by their sum over all
+ *     slabs (MPI_Allreduce); called for the lattice sums of every
+ *     conformal drift and kick and of lat_energies.
+ * A hook returns 0 on success; any other value stops the call with
+ * LAT_ERR_STATE.  Without hooks the evolution calls return LAT_ERR_STATE.
+ * Spectra, Laplacian, initial-condition, checkpoint, output-cube, LOG.out,
+ * autotune and closure calls return LAT_ERR_UNSUPPORTED on a slab handle. */
+typedef int (*lat_halo_fn)(void* user, lat_t* h);
+typedef int (*lat_sum_fn)(void* user, double* v, int32_t n);
+int lat_slab_create(lat_t** out, const lat_config* global_cfg, int32_t z0, int32_t z1);
+int lat_slab_set_hooks(lat_t* h, lat_halo_fn halo, lat_sum_fn sum, void* user);
+/* Bytes of one halo message: one z-plane of every field (FP32 lattices: the
+ * high words phi_hi the stencil reads) and of the six GW strains, in the
+ * handle's precision, [array][y][x]. */
+int lat_slab_halo_bytes(const lat_t* h, size_t* bytes);
+/* op 0 / 1: copy the lowest / highest interior plane (global z0 / z1-1)
+ * into dev_buf; op 2 / 3: fill the lower / upper ghost plane (global z0-1 /
+ * z1) from dev_buf.  dev_buf is device memory of lat_slab_halo_bytes; the
+ * call returns when the copy has completed. */
+int lat_slab_halo(lat_t* h, int32_t op, void* dev_buf);
+
 /* ---------------------------------------------------------- measurement */
 /* Kernel classes timed with CUDA events on the handle's stream when
  * timing is enabled (one event pair per launch). */

@@ -68,6 +68,10 @@ class LatConfig(C.Structure):
 
 _lib = None
 
+# hooks of a z-slab handle (lat_halo_fn, lat_sum_fn)
+HALO_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_void_p)
+SUM_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_int32)
+
 
 def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     """Loads liblattice.so; raises if it has not been built."""
@@ -135,6 +139,9 @@ def _declare(lib: C.CDLL) -> None:
         "lat_write_energy_line": ([P, C.c_char_p, D], I), "lat_write_spectrum_block": ([P, C.c_char_p], I),
         "lat_write_log_line": ([P, C.c_char_p, D], I),
         "lat_closure_attach": ([P, P, I, I], I), "lat_coarsen": ([P, I, I, P], I),
+        "lat_slab_create": ([C.POINTER(P), C.POINTER(LatConfig), I, I], I),
+        "lat_slab_set_hooks": ([P, HALO_FN, SUM_FN, P], I),
+        "lat_slab_halo_bytes": ([P, C.POINTER(C.c_size_t)], I), "lat_slab_halo": ([P, I, P], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name, None)
@@ -434,6 +441,59 @@ class Lattice:
         _check(_lib.lat_closure_attach(self._h, None if net is None else net._h, every, units))
         self._closure = net  # keeps the network alive while attached
 
+
+
+class SlabLattice(Lattice):
+    """The z-planes [z0, z1) of a global finite-difference lattice
+    (lat_slab_create): one rank's part of a decomposed run.  State arrays
+    cover the slab's interior planes, shaped (nfld, z1 - z0, ny, nx).  The
+    evolution calls need set_hooks(): a halo exchange filling both ghost
+    planes, and an all-reduce of the lattice sums over all slabs."""
+
+    def __init__(self, cfg: LatConfig, z0: int, z1: int):
+        lib = load_library()
+        self.cfg = cfg
+        self._h = C.c_void_p()
+        _check(lib.lat_slab_create(C.byref(self._h), C.byref(cfg), int(z0), int(z1)))
+        self.nx, self.ny, self.nfld = cfg.nx, cfg.ny, cfg.nfld
+        self.nz = int(z1) - int(z0)
+        self.z0, self.z1, self.nz_global = int(z0), int(z1), cfg.nz
+        self.N = self.nx * self.ny * self.nz
+        self._hooks = None
+        self.hook_error = None
+
+    def halo_bytes(self) -> int:
+        n = C.c_size_t()
+        _check(_lib.lat_slab_halo_bytes(self._h, C.byref(n)))
+        return n.value
+
+    def halo(self, op: int, dev_ptr: int) -> None:
+        """op 0/1: lowest/highest interior plane -> device buffer; 2/3: device buffer -> lower/upper ghost."""
+        _check(_lib.lat_slab_halo(self._h, int(op), C.c_void_p(dev_ptr)))
+
+    def set_hooks(self, halo, allreduce) -> None:
+        """halo(slab) fills both ghost planes; allreduce(v: np.ndarray) returns
+        v summed over all slabs.  An exception in a hook stops the engine call
+        with a LatticeError and is kept in ``hook_error``."""
+        def _halo(_user, _h):
+            try:
+                halo(self)
+                return 0
+            except Exception as e:  # noqa: BLE001
+                self.hook_error = e
+                return 1
+
+        def _sum(_user, v, n):
+            try:
+                arr = np.ctypeslib.as_array(v, shape=(n,))
+                arr[:] = allreduce(arr.copy())
+                return 0
+            except Exception as e:  # noqa: BLE001
+                self.hook_error = e
+                return 1
+
+        self._hooks = (HALO_FN(_halo), SUM_FN(_sum))  # referenced for as long as the handle lives
+        _check(_lib.lat_slab_set_hooks(self._h, self._hooks[0], self._hooks[1], None))
 
 class DeviceArray:
     """A flat FP32 device buffer (lat_dev_alloc) for closure data sets."""

@@ -156,19 +156,35 @@ struct lat_s {
   // the same fields, writes only cl_b), joined before the fused kick+drift
   cudaStream_t cl_stream = nullptr;
   cudaEvent_t cl_fork = nullptr, cl_join = nullptr;
+
+  // z-slab of a global lattice (lat_slab_create): storage plane 0 is the
+  // ghost of global plane z0-1, planes 1..nz_loc hold global planes
+  // z0..z1-1, plane nz_loc+1 is the ghost of z1.  Kicks and reductions
+  // cover the interior; the ghost planes are filled through the halo hook
+  // before every kick, and the lattice sums go through the sum hook.
+  bool slab = false;
+  int slab_z0 = 0, slab_nzg = 0, nz_loc = 0;
+  double slab_nd = 0;  // sites of the global lattice
+  lat_halo_fn slab_halo = nullptr;
+  lat_sum_fn slab_sum = nullptr;
+  void* slab_user = nullptr;
 };
 
 namespace {
 
 struct ApiGuard {
-  explicit ApiGuard(lat_s* h) {
+  int64_t* prev;
+  explicit ApiGuard(lat_s* h) : prev(g_launch_counter) {
     if (h) {
       g_launch_counter = &h->launches;
       cudaSetDevice(h->dev);
     }
   }
-  ~ApiGuard() { g_launch_counter = nullptr; }
+  ~ApiGuard() { g_launch_counter = prev; }  // a hook may call back into the library
 };
+
+// The site count of the lattice sums: the global lattice for a z-slab.
+double nd_of(const lat_s* h) { return h->slab ? h->slab_nd : (double)h->N; }
 
 // ---------------------------------------------------------------- timing
 int harvest(lat_s* h) {
@@ -276,7 +292,7 @@ PwArgs pw_base(lat_s* h) {
   a.u = nullptr;
   a.pu = nullptr;
   a.model = model_of(h);
-  a.Nd = (double)h->N;
+  a.Nd = nd_of(h);
   a.conf = conformal(h) ? 1 : 0;
   a.sc = h->sc;
   a.rb = red(h);
@@ -302,11 +318,15 @@ FdArgs fd_base(lat_s* h) {
   a.kappa = h->cfg.gw_coupling;
   a.inv2dx = 1.0 / (2.0 * h->dx);
   a.conf = 0;
-  a.Nd = (double)h->N;
+  a.Nd = nd_of(h);
   a.sc = h->sc;
   a.rb = red(h);
   a.ty = h->fd_ty;
   a.zc = h->fd_zc;
+  if (h->slab) {  // the interior planes; the ghosts are the neighbours' boundary planes
+    a.zlo = 1;
+    a.zhi = 1 + h->nz_loc;
+  }
   return a;
 }
 
@@ -400,7 +420,90 @@ int exec_kd(lat_s* h, double hk, double hg, double hd, bool corr = false, cudaEv
   return LAT_OK;
 }
 
+// ------------------------------------------------------------- z-slabs
+int read_scalars(lat_s* h, DevScalars* out);
+
+// Fill the ghost planes through the caller's hook; the stream's work so far
+// has completed when the hook packs the boundary planes.
+int slab_exchange(lat_s* h) {
+  if (!h->slab_halo) return set_error(LAT_ERR_STATE, "z-slab handle without a halo hook (lat_slab_set_hooks)");
+  CK(cudaStreamSynchronize(h->stream));
+  if (h->slab_halo(h->slab_user, h) != 0) return set_error(LAT_ERR_STATE, "z-slab halo hook failed");
+  return LAT_OK;
+}
+
+// Replace v[0..n) by its sum over all slabs through the caller's hook.
+int slab_allreduce(lat_s* h, double* v, int n) {
+  if (!h->slab_sum) return set_error(LAT_ERR_STATE, "z-slab handle without a sum hook (lat_slab_set_hooks)");
+  if (h->slab_sum(h->slab_user, v, n) != 0) return set_error(LAT_ERR_STATE, "z-slab sum hook failed");
+  return LAT_OK;
+}
+
+// Conformal z-slab: complete the ysclp update of a drift or of a kick from
+// the slab's lattice sums (left in sc->red[13..14] by the deferred kernel)
+// summed over all slabs, with the kernels' own arithmetic:
+// Hamiltonian_fields_kin, ysclp += dt (KE2/N)/a^3, and
+// Hamiltonian_fields_grad_pot (FD), ysclp -= a^3 (GE2/a^2/N + 4 PE/N) dt
+// (Pseudospec/openmp_dev/hamiltonian_conformal.f90:92-118,176-205).
+int slab_friedmann(lat_s* h, bool kick, double step) {
+  DevScalars s;
+  RET(read_scalars(h, &s));
+  if (s.err & 1u) return set_error(LAT_ERR_NAN, "NaN/Inf in a lattice reduction");
+  double v[2] = {s.red[13], s.red[14]};
+  RET(slab_allreduce(h, v, 2));
+  const double Nd = h->slab_nd;
+  double ap, pe = 0;
+  if (!kick) {
+    ap = s.ap + step * (v[0] / Nd) / (s.a * s.a * s.a);
+  } else {
+    const double GE2 = v[0] / (s.a * s.a) / Nd;
+    pe = v[1] / Nd;
+    ap = s.ap - s.a * s.a * s.a * (GE2 + 4.0 * pe) * step;
+    CK(cudaMemcpyAsync(&h->sc->pe, &pe, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(cudaMemcpyAsync(&h->sc->ap, &ap, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));  // the host values above are copied before they go out of scope
+  return LAT_OK;
+}
+
+// The op list of a z-slab, eagerly: every kick after a halo exchange,
+// stencil kicks on the interior planes, drifts over the whole storage (the
+// ghosts' momenta stay zero, so their drift changes nothing), the Friedmann
+// updates of a conformal background from the sums of all slabs.
+int exec_slab(lat_s* h, const std::vector<Op>& ops) {
+  const bool conf = conformal(h);
+  for (const Op& o : ops) {
+    switch (o.t) {
+      case 'D': {
+        PwArgs a = pw_base(h);
+        a.mode = PW_DRIFT;
+        a.hd = o.h;
+        a.defer = conf ? 1 : 0;
+        if (h->cfg.gw) { a.u = h->u[h->ucur]; a.pu = h->pu; }
+        RET(launch_pointwise(a, h->prec, h->stream));
+        if (conf) RET(slab_friedmann(h, false, o.h));
+        break;
+      }
+      case 'K': {
+        RET(slab_exchange(h));
+        FdArgs a = fd_base(h);
+        a.hk = o.h;
+        a.hd = 0;
+        a.conf = conf ? 1 : 0;
+        a.defer = conf ? 1 : 0;
+        RET(launch_fd(a, h->prec, h->stream, nullptr));
+        if (conf) RET(slab_friedmann(h, true, o.h));
+        break;
+      }
+      case 'G': RET(exec_grav(h, o.h)); break;
+      default: break;  // 'M' in Minkowski: clock only
+    }
+  }
+  return LAT_OK;
+}
+
 int exec_plain(lat_s* h, const std::vector<Op>& ops) {
+  if (h->slab) return exec_slab(h, ops);
   for (const Op& o : ops) {
     switch (o.t) {
       case 'D': RET(exec_drift(h, o.h)); break;
@@ -773,8 +876,17 @@ int read_scalars(lat_s* h, DevScalars* out) {
 
 // ball_r2 > 0 (FD lattices): also the sums of LOG.out's rhoball into ball[3]
 int compute_energies(lat_s* h, double* out, double ball_r2 = 0.0, double* ball = nullptr) {
+  if (h->slab) {  // the gradient sums read the ghost planes; no ball sums
+    if (ball) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
+    RET(slab_exchange(h));
+  }
   EnergyArgs e{};
   e.ball_r2 = spectral(h) ? 0.0 : ball_r2;
+  if (h->slab) {
+    const int64_t plane = (int64_t)h->nx * h->ny;
+    e.t_lo = plane;
+    e.t_hi = plane * (1 + h->nz_loc);
+  }
   e.dx = h->dx;
   e.nx = h->nx; e.ny = h->ny; e.nz = h->nz; e.nf = h->nf;
   e.phi = h->fld[h->cur];
@@ -803,9 +915,10 @@ int compute_energies(lat_s* h, double* out, double ball_r2 = 0.0, double* ball =
   RET(read_scalars(h, &s));
   if (s.err & 2u) return set_error(LAT_ERR_TIMEOUT, "a tensor copy of a streamed pass was not completed in time");
   if (s.err & 1u) return set_error(LAT_ERR_NAN, "NaN/Inf in a lattice reduction");
+  if (h->slab) RET(slab_allreduce(h, s.red, 8));  // KE, PE, means, the FD gradient sums and GW sums
   const bool conf = conformal(h);
   const double a = conf ? s.a : 1.0;
-  const double Nd = (double)h->N;
+  const double Nd = nd_of(h);
   const double knorm = conf ? 1.0 / std::pow(a, 6) : 1.0;
   const double elap = 1.0 / (h->dx * h->dx) / h->c[4];
   double ge_raw;  // -sum phi lap phi
@@ -916,6 +1029,12 @@ int symp_graph(lat_s* h, int32_t order, double dt, int32_t nsteps, bool run) {
   double tg[3] = {h->tglobal[0], h->tglobal[1], h->tglobal[2]};
   Emitter em = emitter(h, &ops, tg);
   RET(em.symp(order, dt, nsteps));
+  if (h->slab) {  // the hooks run on the host between the kernels: no graphs
+    if (!run) return LAT_OK;
+    RET(exec_slab(h, ops));
+    std::memcpy(h->tglobal, tg, sizeof(tg));
+    return LAT_OK;
+  }
   const bool graphs = h->use_graphs && !h->timing;
   // a graph holds the closure's buffers and its normalisation by value: it
   // matches only the same network, normalisation, cadence and units
@@ -1216,6 +1335,30 @@ int lat_get_config(const lat_t* h, lat_config* cfg) {
 // reported LAT_ERR_NAN is usable again after a fresh upload.
 static int clear_nan_flag(lat_t* h) { return launch_state_reset(h->sc, h->stream); }
 
+// Interior planes of a z-slab <-> unpadded Fortran-layout host arrays
+// fld(nfld, nx, ny, nz_loc) (pad: the sum of the caller's padding, which
+// must be zero).
+static int slab_copy(lat_t* h, double* fld, int pad_f, double* fldp, int pad_p, bool up) {
+  if (pad_f || pad_p) return set_error(LAT_ERR_UNSUPPORTED, "z-slab arrays take no ghost padding");
+  const int64_t plane = (int64_t)h->nx * h->ny, Ni = plane * h->nz_loc;
+  const size_t bytes = sizeof(double) * (size_t)h->nf * Ni;
+  for (int which = 0; which < 2; ++which) {
+    double* host = which == 0 ? fld : fldp;
+    if (!host) continue;
+    char* hi = static_cast<char*>(which == 0 ? h->fld[h->cur] : h->fldp) + (size_t)plane * h->rsz;
+    char* c = (which == 0 && h->fldc) ? static_cast<char*>(h->fldc) + (size_t)plane * h->rsz : nullptr;
+    if (up) {
+      CK(cudaMemcpyAsync(h->stage, host, bytes, cudaMemcpyHostToDevice, h->stream));
+      RET(launch_aos2soa(h->stage, h->nf, Ni, h->prec, hi, c, h->stream, h->N));
+    } else {
+      RET(launch_soa2aos(hi, c, h->nf, Ni, h->prec, h->stage, h->stream, h->N));
+      CK(cudaMemcpyAsync(host, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  return LAT_OK;
+}
+
 int lat_upload(lat_t* h, const double* fld, int32_t fld_lo, int32_t fld_hi, const double* fldp, int32_t fldp_lo,
                int32_t fldp_hi) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
@@ -1223,6 +1366,8 @@ int lat_upload(lat_t* h, const double* fld, int32_t fld_lo, int32_t fld_hi, cons
   ApiGuard g(h);
   RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)h->nf * h->N));
+  if (h->slab) return slab_copy(h, const_cast<double*>(fld), fld_lo + fld_hi, const_cast<double*>(fldp),
+                                fldp_lo + fldp_hi, true);
   if (fld) {
     const double* d = (fld_lo == 0 && fld_hi == 0) ? mapped_host(fld) : nullptr;
     if (!d) {
@@ -1249,6 +1394,7 @@ int lat_download(lat_t* h, double* fld, int32_t fld_lo, int32_t fld_hi, double* 
   if (fld_lo < 0 || fld_hi < 0 || fldp_lo < 0 || fldp_hi < 0) return set_error(LAT_ERR_ARG, "negative padding");
   ApiGuard g(h);
   RET(ensure_stage(h, (size_t)h->nf * h->N));
+  if (h->slab) return slab_copy(h, fld, fld_lo + fld_hi, fldp, fldp_lo + fldp_hi, false);
   if (fld) {
     double* d = (fld_lo == 0 && fld_hi == 0) ? mapped_host(fld) : nullptr;
     RET(launch_soa2aos(h->fld[h->cur], h->fldc, h->nf, h->N, h->prec, d ? d : h->stage, h->stream));
@@ -1357,6 +1503,7 @@ int lat_sync(lat_t* h) {
 }
 
 int lat_laplacian(lat_t* h, int32_t field, double* out) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !out) return set_error(LAT_ERR_ARG, "null argument");
   if (field < 0 || field >= h->nf) return set_error(LAT_ERR_ARG, "bad field index");
   ApiGuard g(h);
@@ -1403,6 +1550,7 @@ int lat_spectrum_nbins(const lat_t* h, int32_t* ns) {
 }
 
 int lat_spectrum(lat_t* h, int32_t what, int32_t field, int32_t mode, int32_t nbins, double* S, double* W) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !S || !W) return set_error(LAT_ERR_ARG, "null argument");
   if (nbins < 1 || nbins > kMaxBins) return set_error(LAT_ERR_ARG, "nbins out of range");
   if (mode != LAT_SPEC_WEIGHTED && mode != LAT_SPEC_COUNT) return set_error(LAT_ERR_ARG, "bad spectrum mode");
@@ -1421,6 +1569,7 @@ int lat_spectrum(lat_t* h, int32_t what, int32_t field, int32_t mode, int32_t nb
 
 int lat_crossspec(lat_t* h, int32_t what1, int32_t field1, int32_t what2, int32_t field2, int32_t nbins,
                   double* S_re, double* S_im) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !S_re || !S_im) return set_error(LAT_ERR_ARG, "null argument");
   if (nbins < 1 || nbins > kMaxBins) return set_error(LAT_ERR_ARG, "nbins out of range");
   ApiGuard g(h);
@@ -1439,6 +1588,7 @@ int lat_crossspec(lat_t* h, int32_t what1, int32_t field1, int32_t what2, int32_
 }
 
 int lat_gw_spectrum(lat_t* h, int32_t nbins, double* S, double* W) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !S || !W) return set_error(LAT_ERR_ARG, "null argument");
   if (!h->cfg.gw) return set_error(LAT_ERR_STATE, "handle has no GW arrays");
   if (nbins < 1 || nbins > kMaxBins) return set_error(LAT_ERR_ARG, "nbins out of range");
@@ -1470,11 +1620,31 @@ int lat_gw_spectrum(lat_t* h, int32_t nbins, double* S, double* W) {
   return LAT_OK;
 }
 
+// GW strains and momenta of a z-slab's interior planes, [6][nz_loc][ny][nx].
+static int slab_gw_copy(lat_t* h, double* u, double* pu, bool up) {
+  const int64_t plane = (int64_t)h->nx * h->ny, Ni = plane * h->nz_loc;
+  for (int which = 0; which < 2; ++which) {
+    double* host = which == 0 ? u : pu;
+    if (!host) continue;
+    char* base = static_cast<char*>(which == 0 ? h->u[h->ucur] : h->pu);
+    if (up) CK(cudaMemcpyAsync(h->stage, host, sizeof(double) * 6 * Ni, cudaMemcpyHostToDevice, h->stream));
+    for (int gc = 0; gc < 6; ++gc) {
+      char* dev = base + ((size_t)gc * h->N + plane) * h->rsz;
+      if (up) RET(launch_from_fp64(h->stage + gc * Ni, Ni, h->prec, dev, nullptr, h->stream));
+      else RET(launch_to_fp64(dev, nullptr, Ni, h->prec, h->stage + gc * Ni, h->stream));
+    }
+    if (!up) CK(cudaMemcpyAsync(host, h->stage, sizeof(double) * 6 * Ni, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  return LAT_OK;
+}
+
 int lat_gw_download(lat_t* h, double* u, double* pu) {
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   if (!h->cfg.gw) return set_error(LAT_ERR_STATE, "handle has no GW arrays");
   ApiGuard g(h);
   RET(ensure_stage(h, (size_t)6 * h->N));
+  if (h->slab) return slab_gw_copy(h, u, pu, false);
   if (u) {
     RET(launch_to_fp64(h->u[h->ucur], nullptr, 6 * h->N, h->prec, h->stage, h->stream));
     CK(cudaMemcpyAsync(u, h->stage, sizeof(double) * 6 * h->N, cudaMemcpyDeviceToHost, h->stream));
@@ -1494,6 +1664,7 @@ int lat_gw_upload(lat_t* h, const double* u, const double* pu) {
   ApiGuard g(h);
   RET(clear_nan_flag(h));
   RET(ensure_stage(h, (size_t)6 * h->N));
+  if (h->slab) return slab_gw_copy(h, const_cast<double*>(u), const_cast<double*>(pu), true);
   if (u) {
     CK(cudaMemcpyAsync(h->stage, u, sizeof(double) * 6 * h->N, cudaMemcpyHostToDevice, h->stream));
     RET(launch_from_fp64(h->stage, 6 * h->N, h->prec, h->u[h->ucur], nullptr, h->stream));
@@ -1508,6 +1679,7 @@ int lat_gw_upload(lat_t* h, const double* u, const double* pu) {
 
 int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0, const double* dfld0, const double* m2eff,
                     double amp, double kcut_frac) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !fld0 || !dfld0 || !m2eff) return set_error(LAT_ERR_ARG, "null argument");
   ApiGuard g(h);
   RET(clear_nan_flag(h));
@@ -1565,6 +1737,7 @@ int lat_init_vacuum(lat_t* h, uint64_t seed, const double* fld0, const double* d
 }
 
 int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0, const double* dfld0, double m2eff, double mpl) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !fld0 || !dfld0 || !(mpl != 0.0)) return set_error(LAT_ERR_ARG, "null or zero argument");
   if (h->nx != h->ny || h->nx != h->nz) return set_error(LAT_ERR_UNSUPPORTED, "sample: cubic lattices");
   ApiGuard g(h);
@@ -1647,6 +1820,7 @@ int lat_init_sample(lat_t* h, uint64_t seed, const double* fld0, const double* d
 }
 
 int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres, double radius, double width) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(width > 0)) return set_error(LAT_ERR_ARG, "bad bubble arguments");
   ApiGuard g(h);
   RET(clear_nan_flag(h));
@@ -1667,6 +1841,7 @@ int lat_init_bubbles(lat_t* h, int32_t nbub, const double* centres, double radiu
 
 int lat_init_bubbles_boosted(lat_t* h, int32_t nbub, const int32_t* centres, double r0, double t0,
                              double phi_false, double phi_true) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || (nbub > 0 && !centres) || nbub < 0 || nbub > 64 || !(r0 >= 0) || !(t0 >= 0))
     return set_error(LAT_ERR_ARG, "bad bubble arguments");
   ApiGuard g(h);
@@ -1691,6 +1866,7 @@ int lat_init_bubbles_boosted(lat_t* h, int32_t nbub, const int32_t* centres, dou
 }
 
 int lat_checkpoint_write(lat_t* h, const char* dir, double time, int32_t frame) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !dir) return set_error(LAT_ERR_ARG, "null argument");
   std::vector<double> f((size_t)h->nf * h->N), p((size_t)h->nf * h->N);
   RET(lat_download(h, f.data(), 0, 0, p.data(), 0, 0));
@@ -1718,6 +1894,7 @@ int lat_checkpoint_write(lat_t* h, const char* dir, double time, int32_t frame) 
 }
 
 int lat_checkpoint_read(lat_t* h, const char* dir, double* time, int32_t* frame) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !dir) return set_error(LAT_ERR_ARG, "null argument");
   std::vector<double> f((size_t)h->nf * h->N), p((size_t)h->nf * h->N);
   for (int l = 0; l < h->nf; ++l) {
@@ -1926,6 +2103,7 @@ int time_pass(lat_s* h, int reps, float* ms) {
 }  // namespace
 
 int lat_autotune(lat_t* h, const char* cache_path) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   const std::string key = tune_key(h);
@@ -2056,6 +2234,7 @@ int lat_autotune(lat_t* h, const char* cache_path) {
 }
 
 int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h) return set_error(LAT_ERR_ARG, "null handle");
   ApiGuard g(h);
   CK(cudaStreamSynchronize(h->stream));
@@ -2091,6 +2270,7 @@ int lat_closure_attach(lat_t* h, lat_net_t* net, int32_t every, int32_t units) {
 }
 
 int lat_coarsen(lat_t* h, int32_t nc, int32_t units, float* out) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !out) return set_error(LAT_ERR_ARG, "null argument");
   ApiGuard g(h);
   if (units != LAT_UNITS_PROGRAM && units != LAT_UNITS_CONFORMAL) return set_error(LAT_ERR_ARG, "units: 0 or 1");
@@ -2191,6 +2371,7 @@ int lat_write_energy_line(lat_t* h, const char* path, double time) {
 }
 
 int lat_write_log_line(lat_t* h, const char* path, double time) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !path) return set_error(LAT_ERR_ARG, "null argument");
   ApiGuard g(h);
   if (spectral(h)) return set_error(LAT_ERR_UNSUPPORTED, "LOG.out: finite-difference lattices");
@@ -2215,6 +2396,7 @@ int lat_write_log_line(lat_t* h, const char* path, double time) {
 }
 
 int lat_write_spectrum_block(lat_t* h, const char* path) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !path) return set_error(LAT_ERR_ARG, "null argument");
   int32_t ns = 0;
   RET(lat_spectrum_nbins(h, &ns));
@@ -2238,6 +2420,7 @@ int lat_write_spectrum_block(lat_t* h, const char* path) {
 
 int lat_write_cube(lat_t* h, int32_t what, int32_t field, int32_t ds, const char* dir, const char* name,
                    int32_t frame, double time) {
+  if (h && h->slab) return set_error(LAT_ERR_UNSUPPORTED, "not available on a z-slab handle");
   if (!h || !dir || !name) return set_error(LAT_ERR_ARG, "null argument");
   if (ds < 1 || h->nx % ds || h->ny % ds || h->nz % ds) return set_error(LAT_ERR_ARG, "sides must be multiples of ds");
   if (frame < 0 || frame > 99999) return set_error(LAT_ERR_ARG, "frame: 0..99999");
@@ -2292,3 +2475,62 @@ int lat_tuning_get(const lat_t* h, int32_t out[6]) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ z-slabs
+int lat_slab_create(lat_t** out, const lat_config* gcfg, int32_t z0, int32_t z1) {
+  if (!out || !gcfg) return set_error(LAT_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (gcfg->laplacian == LAT_LAP_SPECTRAL)
+    return set_error(LAT_ERR_UNSUPPORTED,
+                     "z-slabs need a finite-difference stencil (no distributed transform for the spectral Laplacian)");
+  if (z0 < 0 || z1 <= z0 || z1 > gcfg->nz) return set_error(LAT_ERR_ARG, "slab planes outside [0, nz)");
+  lat_config c = *gcfg;
+  c.nz = (z1 - z0) + 2;  // the interior and one ghost plane on each side
+  c.spectral_impl = LAT_SPEC_IMPL_AUTO;
+  lat_t* h = nullptr;
+  RET(lat_create(&h, &c));
+  h->slab = true;
+  h->slab_z0 = z0;
+  h->slab_nzg = gcfg->nz;
+  h->nz_loc = z1 - z0;
+  h->slab_nd = (double)gcfg->nx * gcfg->ny * gcfg->nz;
+  h->use_graphs = false;
+  *out = h;
+  return LAT_OK;
+}
+
+int lat_slab_set_hooks(lat_t* h, lat_halo_fn halo, lat_sum_fn sum, void* user) {
+  if (!h) return set_error(LAT_ERR_ARG, "null handle");
+  if (!h->slab) return set_error(LAT_ERR_STATE, "not a z-slab handle");
+  h->slab_halo = halo;
+  h->slab_sum = sum;
+  h->slab_user = user;
+  return LAT_OK;
+}
+
+int lat_slab_halo_bytes(const lat_t* h, size_t* bytes) {
+  if (!h || !bytes) return set_error(LAT_ERR_ARG, "null argument");
+  if (!h->slab) return set_error(LAT_ERR_STATE, "not a z-slab handle");
+  *bytes = (size_t)(h->nf + (h->cfg.gw ? 6 : 0)) * h->nx * h->ny * h->rsz;
+  return LAT_OK;
+}
+
+int lat_slab_halo(lat_t* h, int32_t op, void* dev_buf) {
+  if (!h || !dev_buf) return set_error(LAT_ERR_ARG, "null argument");
+  if (!h->slab) return set_error(LAT_ERR_STATE, "not a z-slab handle");
+  if (op < 0 || op > 3) return set_error(LAT_ERR_ARG, "halo op must be 0..3");
+  ApiGuard g(h);
+  const size_t pb = (size_t)h->nx * h->ny * h->rsz;  // bytes of one plane of one array
+  const int pl = op == 0 ? 1 : (op == 1 ? h->nz_loc : (op == 2 ? 0 : h->nz_loc + 1));
+  const int narr = h->nf + (h->cfg.gw ? 6 : 0);
+  for (int k = 0; k < narr; ++k) {
+    char* base = k < h->nf ? static_cast<char*>(h->fld[h->cur]) + (size_t)k * h->N * h->rsz
+                           : static_cast<char*>(h->u[h->ucur]) + (size_t)(k - h->nf) * h->N * h->rsz;
+    char* dev = base + (size_t)pl * pb;
+    char* buf = static_cast<char*>(dev_buf) + (size_t)k * pb;
+    if (op < 2) CK(cudaMemcpyAsync(buf, dev, pb, cudaMemcpyDeviceToDevice, h->stream));
+    else CK(cudaMemcpyAsync(dev, buf, pb, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return LAT_OK;
+}

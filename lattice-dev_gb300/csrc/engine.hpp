@@ -61,6 +61,10 @@ struct FdArgs {
   RedBuf rb;
   int ty, zc;          // tile: 32 x ty threads, zc planes per block
   int vec;             // set by the launcher: 16-byte staging of the tile rows (FP32, nx % 32 == 0)
+  // planes [zlo, zhi) are updated and reduced (zhi = 0: all nz planes); a
+  // z-slab keeps ghost planes 0 and nz-1, filled by the halo exchange
+  int zlo, zhi;
+  int defer;           // conformal kick: store the lattice sums in sc->red[13..14], leave ysclp to the host
 };
 int launch_fd(const FdArgs& a, int precision, cudaStream_t s, int* nblocks_out);
 int fd_max_blocks(int nx, int ny, int nz, int ty, int zc);
@@ -90,6 +94,7 @@ struct PwArgs {
   const float* corr;
   double corr_ts[2];
   int corr_units;  // 0: a^4 (program units), 1: a (conformal units)
+  int defer;       // conformal drift: store sum pi^2 and sum V in sc->red[13..14], leave ysclp to the host
 };
 int launch_pointwise(const PwArgs& a, int precision, cudaStream_t s);
 
@@ -214,10 +219,11 @@ int launch_grav(DevScalars* sc, double h, cudaStream_t s);
 int launch_state_reset(DevScalars* sc, cudaStream_t s);
 
 // ------------------------------------------------------- output kernels
+// fstride: elements between the fields of the SoA arrays (default N)
 int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c,
-                   cudaStream_t s);
+                   cudaStream_t s, int64_t fstride = 0);
 int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos,
-                   cudaStream_t s);
+                   cudaStream_t s, int64_t fstride = 0);
 int launch_to_fp64(const void* hi, const void* c, int64_t n, int precision, double* out, cudaStream_t s);
 int launch_cube(const void* hi, const void* c, int nx, int ny, int nz, int ds, int precision, double* out,
                 cudaStream_t s);
@@ -268,6 +274,7 @@ struct EnergyArgs {
   DevScalars* sc;
   RedBuf rb;
   int grid, block;
+  int64_t t_lo, t_hi;  // sites [t_lo, t_hi) are summed (t_hi = 0: all); a z-slab sums its interior planes
 };
 int launch_energy(const EnergyArgs& a, int precision, cudaStream_t s);
 // sum over the half spectrum of w k^2 |F|^2 (Parseval) into sc->red[slot]

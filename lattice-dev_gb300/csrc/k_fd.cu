@@ -61,8 +61,9 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = tx + TX * ty, nthr = TX * TY;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = blockIdx.z * a.zc;
-  const int z1 = min(z0 + a.zc, nz);
+  const int zend = a.zhi > 0 ? a.zhi : nz;  // planes [a.zlo, zend) are computed
+  const int z0 = a.zlo + blockIdx.z * a.zc;
+  const int z1 = min(z0 + a.zc, zend);
   const int x = x0 + tx, y = y0 + ty;
   const bool active = (x < nx) && (y < ny);
 
@@ -285,12 +286,18 @@ __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
     double tot[2];
     if (grid_reduce<2>(v, a.rb, tot)) {
       DevScalars* sc = a.sc;
-      const double ac = sc->a;
-      const double GE2 = tot[0] / (ac * ac) / a.Nd;
-      const double PE = tot[1] / a.Nd;
-      if (bad(GE2) || bad(PE)) sc->err |= 1u;
-      sc->ap = sc->ap - ac * ac * ac * (GE2 + 4.0 * PE) * a.hk;
-      sc->pe = PE;
+      if (a.defer) {  // a z-slab: the sums of all slabs complete the update on the host
+        sc->red[13] = tot[0];
+        sc->red[14] = tot[1];
+        if (bad(tot[0]) || bad(tot[1])) sc->err |= 1u;
+      } else {
+        const double ac = sc->a;
+        const double GE2 = tot[0] / (ac * ac) / a.Nd;
+        const double PE = tot[1] / a.Nd;
+        if (bad(GE2) || bad(PE)) sc->err |= 1u;
+        sc->ap = sc->ap - ac * ac * ac * (GE2 + 4.0 * PE) * a.hk;
+        sc->pe = PE;
+      }
     }
   }
 }
@@ -302,7 +309,9 @@ int go(const FdArgs& a0, cudaStream_t s, int* nb) {
   a.vec = (sizeof(R) == 4 && a.nx % 32 == 0) ? 1 : 0;  // whole 32-value rows, 16-byte aligned
   const int wd = a.vec ? 40 : 34;
   dim3 block(32, a.ty);
-  dim3 grid((a.nx + 31) / 32, (a.ny + a.ty - 1) / a.ty, (a.nz + a.zc - 1) / a.zc);
+  const int nzc = (a.zhi > 0 ? a.zhi : a.nz) - a.zlo;  // planes computed
+  if (a.zlo < 0 || nzc < 1 || a.zlo + nzc > a.nz) return set_error(LAT_ERR_ARG, "FD plane range");
+  dim3 grid((a.nx + 31) / 32, (a.ny + a.ty - 1) / a.ty, (nzc + a.zc - 1) / a.zc);
   size_t smem = (size_t)3 * NC * wd * (a.ty + 2) * sizeof(R);
   if (a.ty < 1 || (!a.vec && 34 * (a.ty + 2) > kFdMaxSlots * 32 * a.ty))
     return set_error(LAT_ERR_ARG, "FD tile too narrow");

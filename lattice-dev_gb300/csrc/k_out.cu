@@ -8,25 +8,27 @@ namespace {
 // ------------------------------------------------------------ layouts
 // Fortran fld(nfld, i, j, k) (field fastest) <-> device [field][z][y][x].
 template <typename R, bool KAHAN>
-__global__ void aos2soa_kernel(const double* __restrict__ aos, int nf, int64_t N, R* hi, R* c) {
+// fs: element stride between fields of the SoA side (N, or the plane count
+// of a z-slab's storage times the plane size when N covers its interior)
+__global__ void aos2soa_kernel(const double* __restrict__ aos, int nf, int64_t N, int64_t fs, R* hi, R* c) {
   const int64_t tot = N * nf;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = t / nf;
     const int f = (int)(t - s * nf);
     const double v = aos[t];
     const R h = (R)v;
-    hi[f * N + s] = h;
-    if (KAHAN && c) c[f * N + s] = (R)((double)h - v);
+    hi[f * fs + s] = h;
+    if (KAHAN && c) c[f * fs + s] = (R)((double)h - v);
   }
 }
 template <typename R, bool KAHAN>
-__global__ void soa2aos_kernel(const R* hi, const R* c, int nf, int64_t N, double* __restrict__ aos) {
+__global__ void soa2aos_kernel(const R* hi, const R* c, int nf, int64_t N, int64_t fs, double* __restrict__ aos) {
   const int64_t tot = N * nf;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = t / nf;
     const int f = (int)(t - s * nf);
-    double v = (double)hi[f * N + s];
-    if (KAHAN && c) v -= (double)c[f * N + s];
+    double v = (double)hi[f * fs + s];
+    if (KAHAN && c) v -= (double)c[f * fs + s];
     aos[t] = v;
   }
 }
@@ -224,10 +226,13 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
   Acc s[11];
   const R c0 = (R)a.c[0], c1 = (R)a.c[1], c2 = (R)a.c[2], c3 = (R)a.c[3];
   int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool ranged = a.t_hi > 0;  // a z-slab: only its interior sites
+  const int64_t tend = ranged ? a.t_hi : N;
+  if (ranged) t0 += a.t_lo;
   if constexpr (sizeof(R) == 4) {
     // spectral, no GW arrays: four sites per thread and step (float4 loads),
     // one compensated add per sum and four sites
-    if (!a.fd && !u && N % 4 == 0) {  // every field's array starts 16-byte aligned
+    if (!ranged && !a.fd && !u && N % 4 == 0) {  // every field's array starts 16-byte aligned
       const int64_t n4 = N / 4;
       for (int64_t v = t0; v < n4; v += (int64_t)gridDim.x * blockDim.x) {
         float4 fq[NF], pq[NF];
@@ -259,7 +264,7 @@ __global__ void __launch_bounds__(256) energy_kernel(EnergyArgs a) {
       t0 = N;  // no tail
     }
   }
-  for (int64_t t = t0; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = t0; t < tend; t += (int64_t)gridDim.x * blockDim.x) {
     R f[NF];
 #pragma unroll
     for (int l = 0; l < NF; ++l) {
@@ -567,14 +572,21 @@ int launch_bubbles_boosted(double* phi, double* pi, int nx, int ny, int nz, doub
   return done("boosted bubbles");
 }
 
-int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c, cudaStream_t s) {
-  if (precision == LAT_FP64) aos2soa_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, (double*)hi, nullptr);
-  else aos2soa_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, (float*)hi, (float*)c);
+int launch_aos2soa(const double* aos, int nf, int64_t N, int precision, void* hi, void* c, cudaStream_t s,
+                   int64_t fstride) {
+  const int64_t fs = fstride > 0 ? fstride : N;
+  if (precision == LAT_FP64)
+    aos2soa_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, fs, (double*)hi, nullptr);
+  else aos2soa_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>(aos, nf, N, fs, (float*)hi, (float*)c);
   return done("aos2soa");
 }
-int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos, cudaStream_t s) {
-  if (precision == LAT_FP64) soa2aos_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>((const double*)hi, nullptr, nf, N, aos);
-  else soa2aos_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>((const float*)hi, (const float*)c, nf, N, aos);
+int launch_soa2aos(const void* hi, const void* c, int nf, int64_t N, int precision, double* aos, cudaStream_t s,
+                   int64_t fstride) {
+  const int64_t fs = fstride > 0 ? fstride : N;
+  if (precision == LAT_FP64)
+    soa2aos_kernel<double, false><<<grid_for(N * nf), 256, 0, s>>>((const double*)hi, nullptr, nf, N, fs, aos);
+  else
+    soa2aos_kernel<float, true><<<grid_for(N * nf), 256, 0, s>>>((const float*)hi, (const float*)c, nf, N, fs, aos);
   return done("soa2aos");
 }
 // Every ds-th site of one field array as FP64 (phi_hi - c for FP32), in the

@@ -224,9 +224,14 @@ __global__ void __launch_bounds__(256) pw_kernel(PwArgs a) {
         sc->pe = tot[1] / a.Nd;
         sc->ke2 = tot[0];
       } else if (MODE == PW_DRIFT) {
-        sc->ap = co.ap0 + a.hd * (tot[0] / a.Nd) / (co.a0 * co.a0 * co.a0);
-        sc->pe = tot[1] / a.Nd;
-        sc->ke2 = tot[0];
+        if (a.defer) {  // a z-slab: the sums of all slabs complete the update on the host
+          sc->red[13] = tot[0];
+          sc->red[14] = tot[1];
+        } else {
+          sc->ap = co.ap0 + a.hd * (tot[0] / a.Nd) / (co.a0 * co.a0 * co.a0);
+          sc->pe = tot[1] / a.Nd;
+          sc->ke2 = tot[0];
+        }
       } else {
         const double GE2 = tot[2] / (co.a0 * co.a0) / a.Nd;
         const double PE = tot[1] / a.Nd;

@@ -7,9 +7,11 @@ Discrete/Bubble-Collisions/scafld.f90:120-192) and MPI_Allreduce of the
 lattice sums that feed the Friedmann update (hamiltonian_conformal.f90:112-114,
 198-201).  This module is that layer for GB300 machines: a ``Transport``
 interface (implemented over torch.distributed: NCCL between GPUs, gloo between
-CPU ranks for tests), a z-slab decomposition and the halo exchange.  On a
-machine with one GPU the engine runs replicas; the exchange logic is
-exercised by CPU ranks.
+CPU ranks), a z-slab decomposition, the halo exchange of numpy slabs, and
+``engine_slab_hooks``, which drives the CUDA engine's own z-slab handles
+(``SlabLattice``, lat_slab_create) through a Transport: the engine packs its
+boundary planes into device buffers and calls back for the exchange before
+every kick and for the all-reduce of every conformal lattice sum.
 """
 from __future__ import annotations
 
@@ -35,33 +37,60 @@ class Transport:
 
 
 class TorchTransport(Transport):
-    """Transport over an initialised torch.distributed process group."""
+    """Transport over an initialised torch.distributed process group.
+
+    NCCL moves CUDA tensors only: with an NCCL group every message is staged
+    through this rank's current CUDA device (and host arrays are copied back);
+    with gloo the messages stay on the host."""
 
     def __init__(self, group=None):
+        import torch
         import torch.distributed as dist
+        self.torch = torch
         self.dist = dist
         self.group = group
         self.rank = dist.get_rank(group)
         self.size = dist.get_world_size(group)
+        self.backend = str(dist.get_backend(group)).lower()
+        self.device = (torch.device("cuda", torch.cuda.current_device()) if self.backend == "nccl"
+                       else torch.device("cpu"))
+
+    def _wire(self, x: np.ndarray):
+        return self.torch.from_numpy(np.ascontiguousarray(x, np.float64).copy()).to(self.device)
 
     def allreduce_sum(self, x: np.ndarray) -> np.ndarray:
-        import torch
-        t = torch.from_numpy(np.ascontiguousarray(x, np.float64).copy())
+        t = self._wire(x)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
-        return t.numpy()
+        return t.cpu().numpy()
 
     def sendrecv(self, send: np.ndarray, dest: int, recv: np.ndarray, src: int) -> None:
-        import torch
-        s = torch.from_numpy(np.ascontiguousarray(send, np.float64).copy())
-        r = torch.empty(recv.shape, dtype=torch.float64)
         if self.size == 1:
             recv[...] = send
             return
+        s = self._wire(send)
+        r = self.torch.empty(recv.shape, dtype=self.torch.float64, device=self.device)
+        self._p2p(s, dest, r, src)
+        recv[...] = r.cpu().numpy()
+
+    def sendrecv_tensor(self, send, dest: int, recv, src: int) -> None:
+        """send/recv: torch tensors on any device; the transfer runs on the
+        group's device (CUDA for NCCL, the host for gloo)."""
+        if self.size == 1:
+            recv.copy_(send)
+            return
+        s = send if send.device == self.device else send.to(self.device)
+        r = recv if recv.device == self.device else self.torch.empty_like(recv, device=self.device)
+        self._p2p(s, dest, r, src)
+        if r is not recv:
+            recv.copy_(r)
+
+    def _p2p(self, s, dest, r, src):
         ops = [self.dist.P2POp(self.dist.isend, s, dest, self.group),
                self.dist.P2POp(self.dist.irecv, r, src, self.group)]
         for req in self.dist.batch_isend_irecv(ops):
             req.wait()
-        recv[...] = r.numpy()
+        if self.device.type == "cuda":
+            self.torch.cuda.synchronize(self.device)
 
     def barrier(self) -> None:
         self.dist.barrier(self.group)
@@ -156,3 +185,30 @@ def leapfrog_phi4(tr: Transport, slab: Slab, fld: np.ndarray, fldp: np.ndarray, 
     pe = np.sum(0.25 * lam * f ** 4)
     tot = tr.allreduce_sum(np.array([ke, pe]))
     return f, p, tot
+
+
+def engine_slab_hooks(tr: Transport, lat, device=None):
+    """Hooks (halo, allreduce) for an engine z-slab handle ``lat``
+    (``SlabLattice``) whose ranks form a periodic ring in z: before every kick
+    the highest interior plane goes to the rank above, whose lower ghost it
+    fills, and the lowest to the rank below; lattice sums are all-reduced.
+    The halo messages live in device buffers of ``lat_slab_halo_bytes``."""
+    import torch
+    dev = device if device is not None else torch.device("cuda", lat.cfg.device)
+    nb = lat.halo_bytes()
+    lo, hi, glo, ghi = (torch.empty(nb, dtype=torch.uint8, device=dev) for _ in range(4))
+    up, down = (tr.rank + 1) % tr.size, (tr.rank - 1) % tr.size
+
+    def halo(s):
+        s.halo(0, lo.data_ptr())   # the call returns once the copy has completed
+        s.halo(1, hi.data_ptr())
+        tr.sendrecv_tensor(hi, up, glo, down)
+        tr.sendrecv_tensor(lo, down, ghi, up)
+        torch.cuda.synchronize(dev)  # the received planes are in place before the engine reads them
+        s.halo(2, glo.data_ptr())
+        s.halo(3, ghi.data_ptr())
+
+    def allreduce(v: np.ndarray) -> np.ndarray:
+        return tr.allreduce_sum(v)
+
+    return halo, allreduce
