@@ -484,6 +484,9 @@ def diagnostics(L, g, args, dt, ms_step):
     if not args.no_fd:
         out["fd_workloads"] = fd_workloads(L, hbm)
         out["ensemble"] = ensemble_workload(L, 100)
+    # ---- the learned closure on the preheating model (a reduced form of the closure benchmark)
+    if not args.no_closure:
+        out["closure"] = closure_workload(L, args)
     # ---- CPU restatement on the host cores
     if not args.no_cpu:
         rate, cores, done, el = cpu_rate(steps_budget_s=args.cpu_budget, max_steps=args.cpu_steps)
@@ -492,6 +495,68 @@ def diagnostics(L, g, args, dt, ms_step):
                                          f"({el:.1f} s) after 1 warm-up step; CPU restatement of the "
                                          "Fortran reference, OpenMP"}
     return out
+
+
+def closure_workload(L, args):
+    """The learned closure on the two-field preheating model of the headline
+    (V = phi^4/4 + g2 phi^2 chi^2/2, g2 = 2, L = 10 pi, conformal, Yoshida-4,
+    dt = dx/20 on each lattice), fine lattice filtered 4x (sharp k) to the
+    coarse one, evolved to the headline workload's horizon (5000 steps of the
+    256^3 lattice, t = 30.7).  Training data from --closure-train-seeds fine
+    runs (snapshots from t = 5), the network trained by its own BF16 kernels,
+    then --closure-eval-seeds held-out seeds evolved fine, plain coarse and
+    coarse with the closure: P(k) errors of phi and chi against the filtered
+    fine run up to half the coarse Nyquist wavenumber, and times to solution
+    (CUDA events around each evolution).  The full benchmark's sizes (512^3 ->
+    128^3, 64 + 16 seeds) are `--case closure` arguments."""
+    import tempfile
+    C = importlib.import_module("lattice-dev_gb300.closure")
+    nf, nc = args.closure_n_fine, args.closure_n_fine // 4
+    tune = tempfile.NamedTemporaryFile(prefix="lat_tune_", suffix=".jsonl", delete=False).name
+    s = C.Setup(n_fine=nf, n_coarse=nc, tune_cache=tune)
+    t_end = 5000 * s.dt(256)
+    train_seeds = list(range(100, 100 + args.closure_train_seeds))
+    eval_seeds = list(range(900, 900 + args.closure_eval_seeds))
+    t0 = time.perf_counter()
+    ds = C.generate(s, train_seeds, 5.0, t_end, 9)
+    t_gen = time.perf_counter() - t0
+    net = L.Net(seed=11)
+    C.fit_norm(s, ds, net)
+    order = np.random.default_rng(0).permutation(ds.count)
+    n_hold = max(1, ds.count // 8)
+    hold, tr = order[:n_hold], order[n_hold:]
+    t0 = time.perf_counter()
+    hist = C.train(s, ds, net, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, lr_end=args.lr / 10)
+    t_train = time.perf_counter() - t0
+    fe = C.force_error(s, ds, net, hold)
+    ev = C.evaluate(s, net, eval_seeds, t_end, every=args.every, t_attach=0.0)
+    ds.buf.close()
+    net.close()
+    try:
+        os.unlink(tune)
+    except OSError:
+        pass
+    summ = {}
+    for nm in ("plain", "closure"):
+        summ[nm] = {
+            "pk_max_rel_err": np.mean([e[nm]["pk_max_rel_err"] for e in ev], axis=0).tolist(),
+            "pk_mean_rel_err": np.mean([e[nm]["pk_mean_rel_err"] for e in ev], axis=0).tolist(),
+            "time_s": float(np.mean([e[nm]["time_s"] for e in ev]))}
+    t_fine = float(np.mean([e["fine_time_s"] for e in ev]))
+    worst = max(max(summ["closure"]["pk_max_rel_err"]), 0.0)
+    return {"model": "two-field preheating (headline model), conformal", "n_fine": nf, "n_coarse": nc,
+            "t_eval": t_end, "train_seeds": len(train_seeds), "eval_seeds": len(eval_seeds),
+            "samples": ds.count, "heldout_samples": int(n_hold), "epochs": args.epochs,
+            "loss_first_last": [hist[0], hist[-1]], "heldout_force_err": list(map(float, fe)),
+            "pk_bins": "width 2pi/L up to half the coarse Nyquist wavenumber, fields phi and chi",
+            "plain": summ["plain"], "closure": summ["closure"], "fine_time_s": t_fine,
+            "speedup_closure_vs_fine": t_fine / summ["closure"]["time_s"],
+            "speedup_plain_vs_fine": t_fine / summ["plain"]["time_s"],
+            "target": "closure P(k) within 1% of the filtered fine run at >= 10x lower time to solution",
+            "target_met": bool(worst <= 0.01 and t_fine / summ["closure"]["time_s"] >= 10.0),
+            "data_gen_s": t_gen, "train_s": t_train,
+            "scale_note": f"{nf}^3 -> {nc}^3 with {len(train_seeds)} training and {len(eval_seeds)} held-out seeds "
+                          "(the benchmark's 512^3 -> 128^3 with 64 + 16 seeds runs as --case closure)"}
 
 
 ENSEMBLE_SIZES = [64] * 32 + [96] * 32 + [128] * 24 + [192] * 8
@@ -678,7 +743,7 @@ def closure_scenario(args, name):
     L = _il.import_module("lattice-dev_gb300")
     if name == "preheating":
         # the two-field preheating model from vacuum fluctuations, expanding, conformal units
-        s = C.Setup(n_fine=args.n_fine, n_coarse=args.n or 64)
+        s = C.Setup(n_fine=args.n_fine, n_coarse=args.n or 64, tune_cache=os.environ.get("LAT_TUNE_CACHE"))
         return C, s, args.t_start, args.t_end, args.t_start
     # UV-rich fluctuations (<dphi^2> ~ 0.08) in Minkowski: the unresolved modes act on the
     # resolved ones through a mean-field force
@@ -759,6 +824,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fd", action="store_true")
+    ap.add_argument("--no-closure", action="store_true")
+    ap.add_argument("--closure-n-fine", type=int, default=256)
+    ap.add_argument("--closure-train-seeds", type=int, default=4)
+    ap.add_argument("--closure-eval-seeds", type=int, default=2)
     ap.add_argument("--quick", action="store_true", help="headline number only")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--spectral-impl", default="auto", choices=["auto", "cufft", "separable"])

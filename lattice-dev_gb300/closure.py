@@ -48,6 +48,7 @@ class Setup:
     background: int = L.BG_CONFORMAL
     kcut_frac: float = 0.5  # initial fluctuations up to this fraction of the fine Nyquist wavenumber
     units: int = L.UNITS_CONFORMAL  # variables of the training data and of the attached closure
+    tune_cache: str | None = None  # autotuner cache shared by the fine runs (None: tune every handle)
 
     def config(self, n, precision, impl=L.SPEC_IMPL_AUTO):
         return L.make_config(n, nfld=2, length=self.length, laplacian=L.LAP_SPECTRAL, background=self.background,
@@ -99,7 +100,7 @@ def generate(s: Setup, seeds, t_start, t_end, n_snap, capacity=None, progress=No
     for seed in seeds:
         g = L.Lattice(s.config(s.n_fine, s.fine_precision))
         init_fine(s, g, seed)
-        g.autotune(None)
+        g.autotune(s.tune_cache)
         done = 0
         for t in times:
             k = int(round(t / dt)) - done
@@ -197,7 +198,7 @@ def evaluate(s: Setup, net, seeds, t_eval, every=3, coarse_precision=L.FP32_KAHA
     for seed in seeds:
         f = L.Lattice(s.config(s.n_fine, s.fine_precision))
         init_fine(s, f, seed)
-        f.autotune(None)  # the fine reference runs on the engine's fastest path for its lattice
+        f.autotune(s.tune_cache)  # the fine reference runs on the engine's fastest path for its lattice
         fld0, mom0, _ = coarse_state(s, f, scratch)
         dtf = s.dt(s.n_fine)
         kf = int(round(t_eval / dtf))
