@@ -166,6 +166,10 @@ struct lat_ens_s {
     double dx = 0, dk = 0;
     float2* tw = nullptr;     // W_n^j (streamed separable passes)
     float* shift = nullptr;   // [2][count] zs shift per run: written by pass X / pass Z
+    // the class's streamed passes run on their own stream, forked from and
+    // joined to the ensemble's stream around every kick (graph branches)
+    cudaStream_t side = nullptr;
+    cudaEvent_t done = nullptr;
   };
   std::vector<Cls> cls;
   std::vector<int> run_cls;
@@ -185,6 +189,7 @@ struct lat_ens_s {
   int64_t launches = 0;
   std::vector<EnsGraph> graphs;
   cudaEvent_t marks[16] = {};
+  cudaEvent_t fork = nullptr;  // start of a kick on the ensemble's stream
 };
 
 namespace {
@@ -338,7 +343,7 @@ int ens_sep_pass(lat_ens_s* e, const lat_ens_s::Cls& c, int axis, double hk, dou
   a.shift_b = c.shift + c.count;
   a.sc = e->sc;
   a.rb = e->rb;
-  return launch_sep_runs(a, c.n, axis, e->stream);
+  return launch_sep_runs(a, c.n, axis, c.side ? c.side : e->stream);
 }
 
 int ens_pw_args(lat_ens_s* e, int mode, double hk, double hd, double dto);
@@ -367,12 +372,21 @@ int ens_exec_sep(lat_ens_s* e, const std::vector<Op>& ops, double dto) {
       ECK(cudaGetLastError());
     }
   double pending = lead;
+  // the size classes share no device state on these passes: every kick
+  // forks one branch per class (X, Y, Z of its pairs of runs) and joins them,
+  // so one class's pass tails overlap the others' passes
+  const bool branches = e->fork && e->cls.size() > 1;
   for (const Grp& g : grp) {
+    if (branches) ECK(cudaEventRecord(e->fork, e->stream));
     for (auto& c : e->cls) {
+      if (branches) ECK(cudaStreamWaitEvent(c.side, e->fork, 0));
       ERET(ens_sep_pass(e, c, 0, g.hk, pending, dto));
       ERET(ens_sep_pass(e, c, 1, g.hk, 0.0, dto));
       ERET(ens_sep_pass(e, c, 2, g.hk, 0.0, dto));
+      if (branches) ECK(cudaEventRecord(c.done, c.side));
     }
+    if (branches)
+      for (auto& c : e->cls) ECK(cudaStreamWaitEvent(e->stream, c.done, 0));
     pending = g.hd;
   }
   if (pending != 0.0) ERET(ens_pw_args(e, 1, 0.0, pending, dto));
@@ -452,7 +466,10 @@ int lat_ens_destroy(lat_ens_t* e) {
     }
     if (c.tw) cudaFree(c.tw);
     if (c.shift) cudaFree(c.shift);
+    if (c.side) cudaStreamDestroy(c.side);
+    if (c.done) cudaEventDestroy(c.done);
   }
+  if (e->fork) cudaEventDestroy(e->fork);
   void* bufs[] = {e->phi, e->phic, e->pi, e->lap, e->Fk, e->work, e->sc, e->rb.partials, e->rb.counter,
                   e->spec_part, e->spec_out, e->spec_counter};
   for (void* b : bufs)
@@ -558,7 +575,12 @@ int lat_ens_create(lat_ens_t** out, const lat_config* base, int32_t nruns, const
       e->sep_ok = false;
   }
   if (e->sep_ok) {
+    if ((er = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming)) != cudaSuccess)
+      return bail(cuda_fail(er, "ensemble fork event"));
     for (auto& c : e->cls) {
+      if ((er = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking)) != cudaSuccess ||
+          (er = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(cuda_fail(er, "ensemble class stream"));
       if ((st = alloc((void**)&c.tw, (size_t)c.n * sizeof(float2)))) return bail(st);
       if ((st = alloc((void**)&c.shift, (size_t)2 * c.count * sizeof(float)))) return bail(st);
       std::vector<float> w(2 * c.n);
