@@ -537,22 +537,24 @@ EncodeTiledFn encode_tiled_fn() {
 int lat::encode_stream_tmaps(SepArgs& a, int axis, int lines, int n) {
   EncodeTiledFn enc = encode_tiled_fn();
   if (!enc) return set_error(LAT_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
-  const cuuint64_t nx = (cuuint64_t)a.nx, ny = (cuuint64_t)a.ny, nz = (cuuint64_t)a.nz;
+  const cuuint64_t nx = (cuuint64_t)a.nx, ny = (cuuint64_t)a.ny, nz = (cuuint64_t)a.nz, Ns = nx * ny * nz;
+  const cuuint64_t pairs = a.runs ? (cuuint64_t)(a.nlines / a.pair_lines) : 1;
   const cuuint32_t L = (cuuint32_t)lines, N = (cuuint32_t)n;
-  // zs: both fields interleaved, float2 per site, addressed as floats
-  const cuuint64_t zdim[3] = {2 * nx, ny, nz};
-  const cuuint64_t zstr[2] = {2 * nx * 4, 2 * nx * ny * 4};
-  const cuuint32_t zbox[3] = {2 * L, axis == 1 ? N : 1u, axis == 2 ? N : 1u};
-  const cuuint32_t one[4] = {1, 1, 1, 1};
-  CUresult r = enc(&a.tm_zs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(a.lap), zdim, zstr, zbox, one,
+  const cuuint32_t one[5] = {1, 1, 1, 1, 1};
+  // zs: lines A and B interleaved, float2 per site, addressed as floats; a
+  // pair's array follows the previous pair's
+  const cuuint64_t zdim[4] = {2 * nx, ny, nz, pairs};
+  const cuuint64_t zstr[3] = {2 * nx * 4, 2 * nx * ny * 4, 2 * Ns * 4};
+  const cuuint32_t zbox[4] = {2 * L, axis == 1 ? N : 1u, axis == 2 ? N : 1u, 1};
+  CUresult r = enc(&a.tm_zs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(a.lap), zdim, zstr, zbox, one,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_error(LAT_ERR_CUDA, "tensor map of zs: error " + std::to_string((int)r));
-  // momenta of the two fields, N sites apart
-  const cuuint64_t pdim[4] = {nx, ny, nz, 2};
-  const cuuint64_t pstr[3] = {nx * 4, nx * ny * 4, nx * ny * nz * 4};
-  const cuuint32_t pbox[4] = {L, axis == 1 ? N : 1u, axis == 2 ? N : 1u, 2};
-  r = enc(&a.tm_pi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.pi_out, pdim, pstr, pbox, one,
+  // momenta of lines A and B (the two fields, or the two runs of a pair), Ns sites apart
+  const cuuint64_t pdim[5] = {nx, ny, nz, 2, pairs};
+  const cuuint64_t pstr[4] = {nx * 4, nx * ny * 4, Ns * 4, 2 * Ns * 4};
+  const cuuint32_t pbox[5] = {L, axis == 1 ? N : 1u, axis == 2 ? N : 1u, 2, 1};
+  r = enc(&a.tm_pi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, a.pi_out, pdim, pstr, pbox, one,
           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_error(LAT_ERR_CUDA, "tensor map of the momenta: error " + std::to_string((int)r));

@@ -128,10 +128,10 @@ struct SepArgs {
   int* grid_out;            // host: receives the grid of a streamed pass (or null)
   DevScalars* sc;
   RedBuf rb;
-  // streamed passes Y and Z of two fields: tensor maps of zs (float, dims
-  // {2 nx, ny, nz}, box {2 LINES, N, 1} for Y and {2 LINES, 1, N} for Z) and
-  // of the momenta (dims {nx, ny, nz, 2 fields}, box {LINES, N, 1, 2} or
-  // {LINES, 1, N, 2}); a tile is one TMA load of each and one TMA store
+  // streamed passes Y and Z: tensor maps of zs (float, dims {2 nx, ny, nz,
+  // pairs}, box {2 LINES, N, 1, 1} for Y and {2 LINES, 1, N, 1} for Z) and of
+  // the momenta (dims {nx, ny, nz, 2 lines, pairs}, box {LINES, N, 1, 2, 1}
+  // or {LINES, 1, N, 2, 1}); a tile is one TMA load of each
   CUtensorMap tm_zs;
   CUtensorMap tm_pi;
 };

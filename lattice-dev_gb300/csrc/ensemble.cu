@@ -343,6 +343,7 @@ int ens_sep_pass(lat_ens_s* e, const lat_ens_s::Cls& c, int axis, double hk, dou
   a.shift_b = c.shift + c.count;
   a.sc = e->sc;
   a.rb = e->rb;
+  if (axis > 0) ERET(encode_stream_tmaps(a, axis, sep_runs_lines(c.n, axis), c.n));  // Y, Z: TMA tiles
   return launch_sep_runs(a, c.n, axis, c.side ? c.side : e->stream);
 }
 

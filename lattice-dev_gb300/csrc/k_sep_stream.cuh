@@ -32,14 +32,14 @@
 // warp barriers only.  Passes Y, Z: 32 x-columns per block (128-byte rows of
 // momenta: at 16 columns the strided 64-byte rows ran both passes 4-6%
 // slower), with a second slot for the momenta, which are needed only after
-// the transform; for two fields each slot is filled by one TMA tensor copy
-// (zs: a 3D box, the momenta of both fields: one 4D box) issued by one
-// thread and counted on an mbarrier, for pairs of runs by cp.async.  Every
+// the transform; each slot is filled by one TMA tensor copy (zs: a 4D box,
+// the momenta of both lines: one 5D box) issued by one thread and counted on
+// an mbarrier.  Every
 // update of a tile is written by the block that read it, so the passes also
 // run in place.
 //
-// The two-field chain X, Y, Z, finalize is launched with programmatic
-// dependent launch: each pass starts while its predecessor drains and waits
+// The two-field chain X, Y, Z, finalize (pairs of runs: Y, Z) is launched
+// with programmatic dependent launch: each pass starts while its predecessor drains and waits
 // (griddepcontrol.wait) only before reading what the predecessor writes.
 // Pass X stages the phi and c of its first tile early (last written by the
 // previous pass X), pass Z its first zs tile and that tile's transform (zs
@@ -224,6 +224,14 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
       "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
       : "memory");
 }
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3, int c4) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+      : "memory");
+}
 // order this thread's generic-proxy shared-memory accesses before later
 // async-proxy (TMA) accesses of the same memory
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
@@ -248,44 +256,6 @@ __device__ __forceinline__ int64_t tile_base(const SepArgs& a, int64_t l0, int64
   const uint32_t nx = (uint32_t)a.nx;
   const uint32_t o = r / nx, x0 = r - o * nx;
   return pbase + (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0;
-}
-
-// Passes Y, Z: copy the early inputs (part 0: zs, both lines interleaved as
-// float2, one row of LINES float2 per position) or the late ones (part 1: pi
-// of line A and of line B, rows of LINES floats) of tile `tile` into a slot
-// with 16-byte cp.async copies.  Thread tid copies chunk tid % CPR of rows
-// tid / CPR + j * (THREADS / CPR).
-template <int AXIS, int N>
-__device__ __forceinline__ void stage_load(const SepArgs& a, float* dst, int64_t tile, int part, int tid) {
-  using T = STile<AXIS, N>;
-  const int64_t Ns = (int64_t)a.nx * a.ny * a.nz;
-  const int64_t stride = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
-  int64_t pair;
-  const int64_t base = tile_base<AXIS>(a, tile * T::LINES, pair);
-  if (part == 0) {
-    constexpr int CPR = T::RS / 2;  // 16-byte chunks (two float2) per staged row
-    constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
-    static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
-    const int row0 = tid / CPR, ch = tid % CPR;
-    // zs of the pair in float2 units: pair * Ns + the site offset within the pair
-    const float* src = static_cast<const float*>(a.lap) + 2 * (base - pair * Ns + row0 * stride) + ch * 4;
-    float* d0 = dst + row0 * 2 * T::RS + ch * 4;
-#pragma unroll
-    for (int j = 0; j < STEPS; ++j) cp16(d0 + j * RPJ * 2 * T::RS, src + 2 * j * RPJ * stride);
-  } else {
-    constexpr int CPR = T::RS / 4;  // 16-byte chunks per staged row
-    constexpr int PER = T::ROWS * CPR, STEPS = PER / T::THREADS, RPJ = T::THREADS / CPR;
-    static_assert(PER % T::THREADS == 0 && T::THREADS % CPR == 0, "copies must tile the block");
-    const int row0 = tid / CPR, ch = tid % CPR;
-    const int64_t jstep = RPJ * stride;
-    float* d0 = dst + row0 * T::RS + ch * 4;
-    const float* src = static_cast<const float*>(a.pi) + base + row0 * stride + ch * 4;
-#pragma unroll
-    for (int f = 0; f < 2; ++f) {
-#pragma unroll
-      for (int j = 0; j < STEPS; ++j) cp16(d0 + f * T::ARR + j * RPJ * T::RS, src + f * Ns + j * jstep);
-    }
-  }
 }
 
 // Pass X staging by one warp: the rows of its own 32/P lines of tile `tile`
@@ -485,149 +455,13 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   block_partials<4>(vals, a.rb.partials + SEP_PART_X);
 }
 
-// Passes Y (AXIS 1) and Z (AXIS 2): the y part of the kick; the z part with
-// the potential force, which completes the kick (its ysclp update follows in
-// launch_sep_finalize).
-template <int AXIS, int N, bool RUNS, bool CONF>
-__global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
-    sep_stream_yz(const __grid_constant__ SepArgs a) {
-  using T = STile<AXIS, N>;
-  constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  float* sm = reinterpret_cast<float*>(smraw);
-  float* es = sm + T::E_OFF;
-  float* ls = sm + T::L_OFF;
-  float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
-  float2* tf = reinterpret_cast<float2*>(sm + T::TF_OFF);
-  float2* ti = reinterpret_cast<float2*>(sm + T::TI_OFF);
-  float* fk = sm + T::FK_OFF;
-  const int tid = threadIdx.x, t = tid / LINES, li = tid % LINES;
-  const int64_t ntiles = a.nlines / LINES;
-  const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (my > 0) stage_load<AXIS, N>(a, es, blockIdx.x, 0, tid);
-  cp_commit();
-  if (my > 0) stage_load<AXIS, N>(a, ls, blockIdx.x, 1, tid);
-  cp_commit();
-  build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
-
-  const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
-  const int64_t st = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
-  float* __restrict__ pi_o = static_cast<float*>(a.pi_out);
-  const DevScalars* sc = a.sc;
-  // the scalar block holds the state before this kick's pass X until
-  // launch_sep_finalize runs after pass Z: the shift pass X took (the means)
-  // and, from a, ysclp and sum pi^2, the same coefficients pass X computed
-  float zshA = 0.f, zshB = 0.f;
-  if (!RUNS && AXIS == 2) {
-    zshA = (float)__ldcg(&sc->mean[0]);
-    zshB = (float)__ldcg(&sc->mean[1]);
-  }
-  float ck = (float)a.hk, cv = (float)a.hk;
-  if (CONF) {
-    const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
-    const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // pass X's drift
-    const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
-    ck = (float)(a.hk * a1 * a1);
-    cv = (float)(a.hk * a1 * a1 * a1 * a1);
-  }
-  KSum ge, ke;
-  float nzA = 0.f, nzB = 0.f;  // pairs of runs, pass Z: the next tile's shifts, loaded one tile ahead
-  if (RUNS && AXIS == 2 && my > 0) {
-    const int64_t p0 = (int64_t)blockIdx.x * LINES / a.pair_lines;
-    nzA = __ldcg(a.shift_a + 2 * p0);
-    nzB = __ldcg(a.shift_a + 2 * p0 + 1);
-  }
-  for (int64_t j = 0; j < my; ++j) {
-    const int64_t l0 = ((int64_t)blockIdx.x + j * gridDim.x) * LINES;
-    int64_t pair;
-    const int64_t offA = tile_base<AXIS>(a, l0, pair) + li, offB = Nsite + offA;
-    if (RUNS && AXIS == 2) {
-      zshA = nzA;
-      zshB = nzB;
-      if (j + 1 < my) {
-        const int64_t pn = (l0 + (int64_t)gridDim.x * LINES) / a.pair_lines;
-        nzA = __ldcg(a.shift_a + 2 * pn);
-        nzB = __ldcg(a.shift_a + 2 * pn + 1);
-      }
-    }
-    cp_wait_keep<1>();  // zs of this tile (its momenta may still be in flight)
-    __syncthreads();
-    float vr[Q], vi[Q];
-    float hA[AXIS == 2 ? Q : 1], hB[AXIS == 2 ? Q : 1];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int pos = t + P * q;
-      const float2 z = reinterpret_cast<const float2*>(es)[pos * T::RS + li];
-      vr[q] = z.x;
-      vi[q] = z.y;
-      if constexpr (AXIS == 2) {
-        hA[q] = vr[q] + zshA;  // phi - c
-        hB[q] = vi[q] + zshB;
-      }
-    }
-    if constexpr (RUNS && AXIS == 2) {
-      if (t == 0 && li == 0 && l0 % a.pair_lines == 0) {
-        // site 0 of both runs of the pair: the next pass X's shifts
-        a.shift_b[2 * pair] = hA[0];
-        a.shift_b[2 * pair + 1] = hB[0];
-      }
-    }
-    __syncthreads();
-    if (j + 1 < my) stage_load<AXIS, N>(a, es, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 0, tid);
-    cp_commit();
-    d2_line_tab<N, false, CONF>(vr, vi, t, scr + li * T::LSTRIDE, tf, ti, fk, ge);
-    cp_wait_keep<1>();  // the momenta of this tile
-    __syncthreads();
-    float kes[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int pos = t + P * q;
-      const int64_t sA = offA + (int64_t)pos * st, sB = offB + (int64_t)pos * st;
-      float pA = ls[pos * T::RS + li], pB = ls[T::ARR + pos * T::RS + li];
-      if constexpr (AXIS == 1) {
-        pA = pA + ck * vr[q];
-        pB = pB + ck * vi[q];
-      } else {
-        float dA, dB;
-        if constexpr (RUNS) {  // two independent runs: each its own potential
-          float fa[1] = {hA[q]}, fb[1] = {hB[q]}, da[1], db[1];
-          model_dv<float, 1>(a.model, fa, da);
-          model_dv<float, 1>(a.model, fb, db);
-          dA = da[0];
-          dB = db[0];
-        } else {
-          float ff[2] = {hA[q], hB[q]}, dv[2];
-          model_dv<float, 2>(a.model, ff, dv);
-          dA = dv[0];
-          dB = dv[1];
-        }
-        pA = pA + (ck * vr[q] - cv * dA);
-        pB = pB + (ck * vi[q] - cv * dB);
-        if (CONF) kes[q % 4] += pA * pA + pB * pB;
-      }
-      pi_o[sA] = pA;
-      pi_o[sB] = pB;
-    }
-    if (AXIS == 2 && CONF) ke.add((kes[0] + kes[1]) + (kes[2] + kes[3]));
-    __syncthreads();
-    if (j + 1 < my) stage_load<AXIS, N>(a, ls, (int64_t)blockIdx.x + (j + 1) * gridDim.x, 1, tid);
-    cp_commit();
-  }
-  cp_wait_all();
-  if constexpr (!CONF) return;
-  if constexpr (AXIS == 1) {
-    const FF vals[1] = {ge.red()};
-    block_partials<1>(vals, a.rb.partials + SEP_PART_Y);
-  } else {
-    const FF vals[2] = {ge.red(), ke.red()};
-    block_partials<2>(vals, a.rb.partials + SEP_PART_Z);
-  }
-}
-
-
-// Passes Y and Z of two fields with TMA: a tile's zs rows (64 KB at 256
-// points) and both fields' momentum rows (one 4D box) arrive by one tensor
-// copy each, counted on an mbarrier per slot, issued by one thread; the
+// Passes Y (AXIS 1: the y part of the kick) and Z (AXIS 2: the z part with
+// the potential force, which completes the kick; its ysclp update follows in
+// launch_sep_finalize).  A tile's zs rows (64 KB at 256 points) and both
+// lines' momentum rows arrive by one TMA tensor copy each (zs: a 4D box,
+// the momenta of lines A and B: one 5D box; the last dimension is the pair
+// of runs, 1 for the two fields of a lattice), counted on an mbarrier per
+// slot, issued by one thread; the
 // updated momenta are stored from registers (128-byte rows per warp), so the
 // momentum slot takes the next tile as soon as every thread has read it (a
 // tensor store from the slot would hold the next copy until the store had
@@ -639,7 +473,10 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
 // error word (reported as LAT_ERR_TIMEOUT) and the block leaves.
 // MODEL >= 0: the potential fixed at compile time (the model switch folds
 // away in pass Z); -1: read from the arguments.
-template <int AXIS, int N, bool CONF, int MODEL = -1>
+// RUNS: pairs of one-field runs, each line with its own shift (the run's phi
+// at site 0 after the previous kick, from pass X) and its own potential;
+// pass Z hands the new site-0 values to the next pass X.
+template <int AXIS, int N, bool RUNS, bool CONF, int MODEL = -1>
 __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     sep_stream_yz_tma(const __grid_constant__ SepArgs a) {
   using T = STile<AXIS, N>;
@@ -663,26 +500,33 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   const int tid = threadIdx.x, t = tid / LINES, li = tid % LINES;
   const int64_t ntiles = a.nlines / LINES;
   const int my = ntiles > (int64_t)blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-  // tile -> (first x-column, plane index along the other axis): the lines
-  // of pass Y are (x, z), those of pass Z (x, y)
-  auto coords = [&](int tile, int& x0, int& o) {
-    const uint32_t r = (uint32_t)tile * LINES, nx = (uint32_t)a.nx;
+  // tile -> (pair, first x-column, plane index along the other axis): the
+  // lines of pass Y are (x, z), those of pass Z (x, y)
+  auto coords = [&](int tile, int& pr, int& x0, int& o) {
+    uint32_t r = (uint32_t)tile * LINES;
+    pr = 0;
+    if (RUNS) {
+      const uint32_t pl = (uint32_t)a.pair_lines;
+      pr = (int)(r / pl);
+      r -= (uint32_t)pr * pl;
+    }
+    const uint32_t nx = (uint32_t)a.nx;
     o = (int)(r / nx);
     x0 = (int)(r - (uint32_t)o * nx);
   };
   auto load_zs = [&](int tile) {
-    int x0, o;
-    coords(tile, x0, o);
+    int pr, x0, o;
+    coords(tile, pr, x0, o);
     mbar_expect_tx(&bar[0], ZS_BYTES);
-    if (AXIS == 1) tma_load_3d(es, &a.tm_zs, &bar[0], 2 * x0, 0, o);
-    else tma_load_3d(es, &a.tm_zs, &bar[0], 2 * x0, o, 0);
+    if (AXIS == 1) tma_load_4d(es, &a.tm_zs, &bar[0], 2 * x0, 0, o, pr);
+    else tma_load_4d(es, &a.tm_zs, &bar[0], 2 * x0, o, 0, pr);
   };
   auto load_pi = [&](int tile) {
-    int x0, o;
-    coords(tile, x0, o);
+    int pr, x0, o;
+    coords(tile, pr, x0, o);
     mbar_expect_tx(&bar[1], PI_BYTES);
-    if (AXIS == 1) tma_load_4d(ls, &a.tm_pi, &bar[1], x0, 0, o, 0);
-    else tma_load_4d(ls, &a.tm_pi, &bar[1], x0, o, 0, 0);
+    if (AXIS == 1) tma_load_5d(ls, &a.tm_pi, &bar[1], x0, 0, o, 0, pr);
+    else tma_load_5d(ls, &a.tm_pi, &bar[1], x0, o, 0, 0, pr);
   };
   const int64_t Nsite = (int64_t)a.nx * a.ny * a.nz;
   const int64_t st = AXIS == 1 ? a.nx : (int64_t)a.nx * a.ny;
@@ -714,7 +558,7 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
 
   const DevScalars* sc = a.sc;  // written by the finalize three kernels back
   float zshA = 0.f, zshB = 0.f;
-  if (AXIS == 2) {
+  if (AXIS == 2 && !RUNS) {
     zshA = (float)__ldcg(&sc->mean[0]);
     zshB = (float)__ldcg(&sc->mean[1]);
   }
@@ -726,6 +570,12 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   for (int j = 0; j < my; ++j) {
     const int tile = (int)blockIdx.x + j * (int)gridDim.x;
     const uint32_t ph = (uint32_t)(j & 1);
+    int pr, x0, o;
+    coords(tile, pr, x0, o);
+    if (RUNS && AXIS == 2) {  // the shifts pass X took for the two runs of this pair
+      zshA = __ldcg(a.shift_a + 2 * pr);
+      zshB = __ldcg(a.shift_a + 2 * pr + 1);
+    }
     fail = !mbar_wait(&bar[0], ph);
     if (__syncthreads_or(fail)) break;
     if (CONF && j == 0) {
@@ -745,6 +595,13 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
         hB[q] = vi[q] + zshB;
       }
     }
+    if constexpr (RUNS && AXIS == 2) {
+      if (t == 0 && li == 0 && ((uint32_t)tile * LINES) % (uint32_t)a.pair_lines == 0) {
+        // site 0 of both runs of the pair: the next pass X's shifts
+        a.shift_b[2 * pr] = hA[0];
+        a.shift_b[2 * pr + 1] = hB[0];
+      }
+    }
     __syncthreads();  // every thread has its zs: the slot takes the next tile
     if (tid == 0 && j + 1 < my) {
       fence_proxy_async();
@@ -758,9 +615,8 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     }
     fail = !mbar_wait(&bar[1], ph);
     if (__syncthreads_or(fail)) break;
-    int x0, o;
-    coords(tile, x0, o);
-    const int64_t offA = (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0 + li, offB = Nsite + offA;
+    const int64_t offA = (int64_t)pr * 2 * Nsite + (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0 + li;
+    const int64_t offB = Nsite + offA;
     float kes[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -771,10 +627,21 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
         pA = pA + ck * vr[q];
         pB = pB + ck * vi[q];
       } else {
-        float ff[2] = {hA[q], hB[q]}, dv[2];
-        model_dv<float, 2>(mp, ff, dv);
-        pA = pA + (ck * vr[q] - cv * dv[0]);
-        pB = pB + (ck * vi[q] - cv * dv[1]);
+        float dA, dB;
+        if constexpr (RUNS) {  // two independent runs: each its own potential
+          float fa[1] = {hA[q]}, fb[1] = {hB[q]}, da[1], db[1];
+          model_dv<float, 1>(mp, fa, da);
+          model_dv<float, 1>(mp, fb, db);
+          dA = da[0];
+          dB = db[0];
+        } else {
+          float ff[2] = {hA[q], hB[q]}, dv[2];
+          model_dv<float, 2>(mp, ff, dv);
+          dA = dv[0];
+          dB = dv[1];
+        }
+        pA = pA + (ck * vr[q] - cv * dA);
+        pB = pB + (ck * vi[q] - cv * dB);
         if (CONF) kes[q % 4] += pA * pA + pB * pB;
       }
       pi_o[offA + (int64_t)pos * st] = pA;
@@ -846,40 +713,33 @@ int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
       (RUNS && (a.conf || !a.shift_a || !a.shift_b)))
     return set_error(LAT_ERR_STATE, "streamed separable pass: lines do not form whole tiles");
   const int64_t ntiles = a.nlines / lines;
-  // an expanding background (two fields only) adds the lattice sums of the
-  // Friedmann update; a static one needs none of them
-  constexpr bool PDL = !RUNS;  // the two-field chain X, Y, Z, finalize
+  // X, Y, Z (and the two-field finalize) launch as programmatic dependents;
+  // the pairs-of-runs pass X follows an event join, so it launches plainly
+  using TY = STile<1, N>;
+  using TZ = STile<2, N>;
   if constexpr (!RUNS) {
     if (a.conf) {
       switch (axis) {
         case 0: return stream_launch(sep_stream_x<N, false, true>, STile<0, N>::SMEM, STile<0, N>::THREADS,
-                                     STile<0, N>::MINB, ntiles, a, s, PDL);
-        case 1: return stream_launch(sep_stream_yz_tma<1, N, true>, STile<1, N>::SMEM + 128, STile<1, N>::THREADS,
-                                     STile<1, N>::MINB, ntiles, a, s, PDL);
+                                     STile<0, N>::MINB, ntiles, a, s, true);
+        case 1: return stream_launch(sep_stream_yz_tma<1, N, false, true>, TY::SMEM + 128, TY::THREADS, TY::MINB,
+                                     ntiles, a, s, true);
         default:
           if (a.model.model == LAT_MODEL_PHI4_G2)
-            return stream_launch(sep_stream_yz_tma<2, N, true, LAT_MODEL_PHI4_G2>, STile<2, N>::SMEM + 128,
-                                 STile<2, N>::THREADS, STile<2, N>::MINB, ntiles, a, s, PDL);
-          return stream_launch(sep_stream_yz_tma<2, N, true>, STile<2, N>::SMEM + 128, STile<2, N>::THREADS,
-                               STile<2, N>::MINB, ntiles, a, s, PDL);
+            return stream_launch(sep_stream_yz_tma<2, N, false, true, LAT_MODEL_PHI4_G2>, TZ::SMEM + 128, TZ::THREADS,
+                                 TZ::MINB, ntiles, a, s, true);
+          return stream_launch(sep_stream_yz_tma<2, N, false, true>, TZ::SMEM + 128, TZ::THREADS, TZ::MINB, ntiles,
+                               a, s, true);
       }
     }
   }
-  if constexpr (!RUNS) {
-    if (axis == 1)
-      return stream_launch(sep_stream_yz_tma<1, N, false>, STile<1, N>::SMEM + 128, STile<1, N>::THREADS,
-                           STile<1, N>::MINB, ntiles, a, s, PDL);
-    if (axis == 2)
-      return stream_launch(sep_stream_yz_tma<2, N, false>, STile<2, N>::SMEM + 128, STile<2, N>::THREADS,
-                           STile<2, N>::MINB, ntiles, a, s, PDL);
-  }
   switch (axis) {
     case 0: return stream_launch(sep_stream_x<N, RUNS, false>, STile<0, N>::SMEM, STile<0, N>::THREADS,
-                                 STile<0, N>::MINB, ntiles, a, s, PDL);
-    case 1: return stream_launch(sep_stream_yz<1, N, RUNS, false>, STile<1, N>::SMEM, STile<1, N>::THREADS,
-                                 STile<1, N>::MINB, ntiles, a, s, PDL);
-    default: return stream_launch(sep_stream_yz<2, N, RUNS, false>, STile<2, N>::SMEM, STile<2, N>::THREADS,
-                                  STile<2, N>::MINB, ntiles, a, s, PDL);
+                                 STile<0, N>::MINB, ntiles, a, s, !RUNS);
+    case 1: return stream_launch(sep_stream_yz_tma<1, N, RUNS, false>, TY::SMEM + 128, TY::THREADS, TY::MINB, ntiles,
+                                 a, s, true);
+    default: return stream_launch(sep_stream_yz_tma<2, N, RUNS, false>, TZ::SMEM + 128, TZ::THREADS, TZ::MINB, ntiles,
+                                  a, s, true);
   }
 }
 
