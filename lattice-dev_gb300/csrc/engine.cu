@@ -168,6 +168,11 @@ struct lat_s {
   lat_halo_fn slab_halo = nullptr;
   lat_sum_fn slab_sum = nullptr;
   void* slab_user = nullptr;
+
+  // tensor maps of the streamed passes Y and Z, encoded for the zs and
+  // momentum buffers they were made with
+  CUtensorMap sep_tm_zs[2] = {}, sep_tm_pi[2] = {};
+  const void* sep_tm_for[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
 };
 
 namespace {
@@ -607,8 +612,17 @@ int sep_pass(lat_s* h, int axis, double hk, double hg, double hd, int* grid_out 
   a.runs = 0;                // the two fields of this lattice form one pair
   a.pair_lines = a.nlines;
   if (h->sep_stream && axis > 0) {  // passes Y and Z move their tiles by TMA
-    const int lines = n == 128 ? sep_stream_lines_128(axis) : sep_stream_lines_256(axis);
-    RET(encode_stream_tmaps(a, axis, lines, n));
+    const int k = axis - 1;
+    if (h->sep_tm_for[k][0] != a.lap || h->sep_tm_for[k][1] != a.pi_out) {
+      const int lines = n == 128 ? sep_stream_lines_128(axis) : sep_stream_lines_256(axis);
+      RET(encode_stream_tmaps(a, axis, lines, n));
+      h->sep_tm_zs[k] = a.tm_zs;
+      h->sep_tm_pi[k] = a.tm_pi;
+      h->sep_tm_for[k][0] = a.lap;
+      h->sep_tm_for[k][1] = a.pi_out;
+    }
+    a.tm_zs = h->sep_tm_zs[k];
+    a.tm_pi = h->sep_tm_pi[k];
   }
   int st;
   switch (n) {

@@ -170,6 +170,10 @@ struct lat_ens_s {
     // joined to the ensemble's stream around every kick (graph branches)
     cudaStream_t side = nullptr;
     cudaEvent_t done = nullptr;
+    // tensor maps of passes Y and Z (zs and momenta of the class's pairs),
+    // encoded once: the class's arrays never move
+    CUtensorMap tm_zs[2] = {}, tm_pi[2] = {};
+    bool tm_ok[2] = {false, false};
   };
   std::vector<Cls> cls;
   std::vector<int> run_cls;
@@ -312,7 +316,7 @@ int ens_fft(lat_ens_s* e, bool forward) {
 
 // One streamed separable pass (k_sep_stream.cuh) over every pair of runs of
 // class c: in place, kick weight hk and preceding drift hd in units of dt.
-int ens_sep_pass(lat_ens_s* e, const lat_ens_s::Cls& c, int axis, double hk, double hd, double dto) {
+int ens_sep_pass(lat_ens_s* e, lat_ens_s::Cls& c, int axis, double hk, double hd, double dto) {
   const int64_t n = c.n, n3 = n * n * n;
   const double dt = dto * c.dx;
   SepArgs a{};
@@ -343,7 +347,16 @@ int ens_sep_pass(lat_ens_s* e, const lat_ens_s::Cls& c, int axis, double hk, dou
   a.shift_b = c.shift + c.count;
   a.sc = e->sc;
   a.rb = e->rb;
-  if (axis > 0) ERET(encode_stream_tmaps(a, axis, sep_runs_lines(c.n, axis), c.n));  // Y, Z: TMA tiles
+  if (axis > 0) {  // Y, Z: TMA tiles
+    if (!c.tm_ok[axis - 1]) {
+      ERET(encode_stream_tmaps(a, axis, sep_runs_lines(c.n, axis), c.n));
+      c.tm_zs[axis - 1] = a.tm_zs;
+      c.tm_pi[axis - 1] = a.tm_pi;
+      c.tm_ok[axis - 1] = true;
+    }
+    a.tm_zs = c.tm_zs[axis - 1];
+    a.tm_pi = c.tm_pi[axis - 1];
+  }
   return launch_sep_runs(a, c.n, axis, c.side ? c.side : e->stream);
 }
 
