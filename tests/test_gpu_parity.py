@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_err
-from helpers import L, bubble_fd27, phi4_fd7, two_field_spectral, random_state, vacuum_ic
+from helpers import L, bubble_fd27, cfg, phi4_fd7, two_field_spectral, random_state, vacuum_ic
 
 pytestmark = pytest.mark.gpu
 TOL64 = 1e-10
@@ -328,6 +328,32 @@ def test_pinned_host_arrays_direct(engine, prec):
     finally:
         for p in ptrs:
             engine.host_free(p)
+
+
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32_KAHAN])
+@pytest.mark.parametrize("nf", [1, 2])
+@pytest.mark.parametrize("shape", [(12, 8, 16), (7, 5, 3)])
+def test_layout_conversion_exact(engine, prec, nf, shape):
+    """FP64 host arrays <-> device state, bit for bit: FP64 kept as is; FP32
+    fields as hi = fl32(v), c = fl32(hi - v), read back as hi - c; FP32 momenta
+    as fl32(v), on an even and an odd site count."""
+    nx, ny, nz = shape
+    c = cfg((nx, ny, nz), nfld=nf, length=4.0, laplacian=L.LAP_FD7, background=L.BG_MINKOWSKI, precision=prec,
+            model=L.MODEL_PHI4 if nf == 1 else L.MODEL_PHI4_G2, model_params=(1.0,) if nf == 1 else (1.0, 2.0))
+    g = engine.Lattice(c)
+    rng = np.random.default_rng(17)
+    f = rng.standard_normal((nf, nz, ny, nx)) * np.exp(rng.uniform(-20, 20, (nf, nz, ny, nx)))
+    p = rng.standard_normal((nf, nz, ny, nx))
+    g.set_state(f, p)
+    fb, pb = g.get_state()
+    g.close()
+    if prec == L.FP64:
+        assert np.array_equal(fb, f) and np.array_equal(pb, p)
+        return
+    hi = f.astype(np.float32)
+    cc = (hi.astype(np.float64) - f).astype(np.float32)
+    assert np.array_equal(fb, hi.astype(np.float64) - cc.astype(np.float64))
+    assert np.array_equal(pb, p.astype(np.float32).astype(np.float64))
 
 
 def test_checkpoint_roundtrip(engine, tmp_path):
