@@ -34,9 +34,30 @@ struct DevScalars {
   double mean[4];  // lattice means of the fields (spectral shift of the separable passes)
   double zsh[2];   // shift the zs array of the last streamed kick was taken with (k_sep_stream.cuh)
   double ke_cur;   // sum pi^2 of the current momenta, kept by the streamed passes
+  float co[4];     // FP32 cd, ck, cv of the next streamed kick (kick_coefs_of), from the kernel before it
   unsigned int err;  // bit 0: NaN/Inf met in a reduction; bit 1: a bounded device wait gave up
   unsigned int pad[3];
 };
+
+// The FP32 coefficients of a streamed kick from the FP64 scalar state before
+// it (hamiltonian_conformal.f90:86-174): cd = hd/a0^2 for the drift of pass
+// X, ck = hk a1^2 and cv = hk a1^4 for the kick, where a1 = a0 - hg ap0/6
+// follows the drift's ysclp update ap0 = ap + hd (ke/N)/a0^3.  Evaluated once
+// per kick by the single-block kernel before it (k_spec.cu), never in the
+// passes: at GB300's FP64 rate the chain's divisions and dependent loads held
+// the start of every pass that evaluated it.  One reciprocal of a0 serves
+// every quotient, and 1/N, 1/6 fold into products: each FP64 division is a
+// dependent chain on the critical path between pass Z and the next pass X.
+__device__ __forceinline__ void kick_coefs_of(double a0, double ap, double ke, double hd, double hk, double hg,
+                                              double Nd, float* c) {
+  const double r = 1.0 / a0, r2 = r * r;
+  const double ap0 = ap + hd * ke * (1.0 / Nd) * (r2 * r);
+  const double a1 = a0 - (hg * (1.0 / 6.0)) * ap0;
+  c[0] = (float)(hd * r2);
+  const double k1 = hk * a1 * a1;
+  c[1] = (float)k1;
+  c[2] = (float)(k1 * a1 * a1);
+}
 
 // Reduction scratch: one partial row per block plus an arrival counter.
 struct RedBuf {

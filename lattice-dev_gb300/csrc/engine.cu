@@ -676,11 +676,13 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
     return LAT_ERR_UNSUPPORTED;
   }
   double pending = lead;
-  if (h->sep_stream && conf && !grp.empty()) {  // sum pi^2 for the first pass X
+  if (h->sep_stream && conf && !grp.empty()) {  // sum pi^2 and the coefficients of the first kick
     Timed t(h, LAT_K_OTHER);
-    RET(launch_pi2_sum(h->fldp, (int64_t)h->nf * h->N, h->sc, red(h), 2 * h->nsm, h->stream));
+    RET(launch_pi2_sum(h->fldp, (int64_t)h->nf * h->N, h->sc, red(h), 2 * h->nsm, h->stream,
+                       KickW{grp[0].hk, grp[0].hg, lead, 1}, (double)h->N));
   }
-  for (const Grp& g : grp) {
+  for (size_t gi = 0; gi < grp.size(); ++gi) {
+    const Grp& g = grp[gi];
     if (h->sep_stream) {
       // every streamed pass takes the kick's weights and pass X's drift (the
       // scalar block keeps the pre-kick state until the finalize after Z)
@@ -695,6 +697,8 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
       f.hd = pending;
       f.Nd = (double)h->N;
       f.conf = conf ? 1 : 0;
+      // the next kick takes this group's drift in its pass X
+      if (conf && gi + 1 < grp.size()) f.next = KickW{grp[gi + 1].hk, grp[gi + 1].hg, g.hd, 1};
       if (!conf) f.gy = f.gz = 0;  // a static background writes no Y, Z partials
       if (4 * f.gx > SEP_PART_Y || f.gy > SEP_PART_Z - SEP_PART_Y || (SEP_PART_Z + 2 * f.gz) > 16 * h->red_cap)
         return set_error(LAT_ERR_STATE, "streamed separable passes: partial sums exceed the reduction buffer");

@@ -179,7 +179,14 @@ inline int launch_sep_runs(const SepArgs& a, int n, int axis, cudaStream_t s) {
     default: return set_error(LAT_ERR_UNSUPPORTED, "streamed separable passes: line length");
   }
 }
-int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s);
+// A streamed kick's weights (valid = 0: no kick follows in this call).
+struct KickW {
+  double hk, hg, hd;
+  int valid;
+};
+// sum pi^2 into sc->ke_cur; with first.valid also the first kick's coefficients into sc->co
+int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s,
+                   KickW first = KickW{0.0, 0.0, 0.0, 0}, double Nd = 1.0);
 // Partials of the streamed passes of one kick in the reduction buffer: pass X
 // [grid][pe, GEx, sum phi_A, sum phi_B] at SEP_PART_X, pass Y [grid][GEy],
 // pass Z [grid][GEz, sum pi^2]; completed after pass Z by launch_sep_finalize.
@@ -191,6 +198,7 @@ struct SepFinArgs {
   double hk, hg, hd;   // the kick, its grav-kinetic halves and the drift of pass X
   double Nd;
   int conf;
+  KickW next;          // the next kick of the call, whose coefficients the finalize leaves in sc->co
 };
 int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s);
 int sep_columns_16(int precision, int nf);

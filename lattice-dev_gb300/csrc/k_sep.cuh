@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(256) sep_kernel(SepArgs a) {
   using C = typename Cx<R>::T;
   using T = Tile<R, NF, AXIS, N>;
   constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* twN = reinterpret_cast<C*>(smraw);
   C* fft = twN + N;
   R* astage = reinterpret_cast<R*>(fft + LINES * T::LSTRIDE);  // [NA][ATILE]

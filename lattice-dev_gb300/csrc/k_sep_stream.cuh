@@ -43,10 +43,13 @@
 // (griddepcontrol.wait) only before reading what the predecessor writes.
 // Pass X stages the phi and c of its first tile early (last written by the
 // previous pass X), pass Z its first zs tile and that tile's transform (zs
-// comes from pass X; pass Y writes only the momenta).  The FP64 coefficient
-// chain of a kick is evaluated once per warp (X) or per block (Y, Z), not
-// per thread: at GB300's FP64 rate the per-thread chain had cost pass Z
-// 13 us of its 92 us at 256^3.
+// comes from pass X; pass Y writes only the momenta).  The passes load the
+// kick's FP32 coefficients (cd, ck, cv: kick_coefs_of) from the scalar block,
+// where the single-block kernel before pass X (the previous kick's finalize,
+// or the momentum sum that starts a call) left them: at GB300's FP64 rate the
+// coefficient chain, evaluated per thread, had cost pass Z 13 us of its 92 us
+// at 256^3, and evaluated once per warp (X) or block (Y, Z) it still held
+// each pass's start, 23.5 us per Yoshida-4 step.
 #pragma once
 #include "k_sep.cuh"
 
@@ -260,8 +263,7 @@ __device__ __forceinline__ int64_t tile_base(const SepArgs& a, int64_t l0, int64
 
 // Pass X staging by one warp: the rows of its own 32/P lines of tile `tile`
 // (6 arrays: [line A, B][phi, c, pi]), so the warp waits only for its copies.
-// WHICH: 3 = all six arrays, 1 = phi and c only, 2 = pi only.
-template <int N, int WHICH = 3>
+template <int N>
 __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64_t tile, int warp, int lane) {
   using T = STile<0, N>;
   constexpr int LPW = 32 / T::P, CPR = N / 4;  // lines per warp, 16-byte chunks per row
@@ -272,7 +274,6 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
 #pragma unroll
   for (int arr = 0; arr < 6; ++arr) {
     const int f = arr / 3, k = arr % 3;
-    if (!((k == 2 ? 2 : 1) & WHICH)) continue;
     const void* sp = k == 0 ? a.phi : (k == 1 ? a.phic : a.pi);
     const float* src = static_cast<const float*>(sp) + f * Ns + r0;
 #pragma unroll
@@ -283,43 +284,13 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
   }
 }
 
-// The kick's FP32 coefficients from the scalar block's pre-kick state
-// (hamiltonian_conformal.f90:86-174): cd = hd/a0^2, ck = hk a1^2,
-// cv = hk a1^4 with a1 after the drift's ysclp update and the gravity half
-// step.  GB300's FP64 rate makes the chain cost microseconds when every
-// thread of a block evaluates it, so one thread does: kick_coefs() into
-// shared memory (thread 0, read after the next block barrier), or
-// kick_coefs_warp() in lane 0 of every warp, broadcast by shuffle.
-__device__ __forceinline__ void kick_coefs_eval(const SepArgs& a, float (&c)[3]) {
-  const DevScalars* sc = a.sc;
-  const double a0 = __ldcg(&sc->a), ke = __ldcg(&sc->ke_cur);
-  const double ap0 = __ldcg(&sc->ap) + a.hd * (ke / a.Nd) / (a0 * a0 * a0);  // the drift's ysclp update
-  const double a1 = a0 - a.hg * ap0 / 6.0;                                   // Hamiltonian_grav_kinetic
-  c[0] = (float)(a.hd / (a0 * a0));
-  c[1] = (float)(a.hk * a1 * a1);
-  c[2] = (float)(a.hk * a1 * a1 * a1 * a1);
-}
-__device__ __forceinline__ void kick_coefs(const SepArgs& a, float* coef, int tid) {
-  if (tid != 0) return;
-  float c[3];
-  kick_coefs_eval(a, c);
-  coef[0] = c[0];
-  coef[1] = c[1];
-  coef[2] = c[2];
-}
-__device__ __forceinline__ void kick_coefs_warp(const SepArgs& a, float (&c)[3], int lane) {
-  if (lane == 0) kick_coefs_eval(a, c);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) c[i] = __shfl_sync(0xffffffffu, c[i], 0);
-}
-
 // Pass X: drift, zs and the x part of the kick.
 template <int N, bool RUNS, bool CONF>
 __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     sep_stream_x(const __grid_constant__ SepArgs a) {
   using T = STile<0, N>;
   constexpr int P = T::P, Q = T::Q, LINES = T::LINES;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   float* sm = reinterpret_cast<float*>(smraw);
   float* es = sm + T::E_OFF;
   float2* scr = reinterpret_cast<float2*>(sm + T::S_OFF);
@@ -330,17 +301,17 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   const int64_t ntiles = a.nlines / LINES;
   const int64_t my = ntiles > (int64_t)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   if constexpr (!RUNS) {
-    // launched as a programmatic dependent of the previous kick's finalize:
-    // phi and c were last written by the previous pass X, so the first
-    // tile's phi and c are staged while the predecessor drains; the momenta
-    // (previous pass Z) and the scalar block (finalize) only after the wait
-    if (my > 0) stage_rows_x<N, 1>(a, es, blockIdx.x, warp, lane);
+    // launched as a programmatic dependent of the previous kick's finalize
+    // (or of the momentum sum that starts a call), which lets this pass start
+    // only after its own wait for the kernel before it: phi and c (last
+    // written by the previous pass X) and the momenta (previous pass Z) are
+    // complete, so the whole first tile is staged while the predecessor
+    // runs; the scalar block it writes is read after the wait
+    if (my > 0) stage_rows_x<N>(a, es, blockIdx.x, warp, lane);
     cp_commit();
     build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
     pdl_wait();
     pdl_trigger();
-    if (my > 0) stage_rows_x<N, 2>(a, es, blockIdx.x, warp, lane);
-    cp_commit();
   } else {
     if (my > 0) stage_rows_x<N>(a, es, blockIdx.x, warp, lane);
     cp_commit();
@@ -363,11 +334,9 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   }
   const bool drift = a.hd != 0.0;
   float cd = (float)a.hd, ck = (float)a.hk;
-  if (CONF) {  // the scalar block is read after the wait above
-    float c[3];
-    kick_coefs_warp(a, c, lane);
-    cd = c[0];
-    ck = c[1];
+  if (CONF) {  // the kick's coefficients, left by the kernel before it (read after the wait above)
+    cd = __ldcg(&sc->co[0]);
+    ck = __ldcg(&sc->co[1]);
   }
   KSum ge, pe, mA, mB;
   // pairs of runs: each run's shift is its phi at site 0 after the previous
@@ -486,7 +455,6 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
   static_assert(T::E_OFF == 0 && (T::L_OFF * 4) % 128 == 0, "TMA slots must be 128-byte aligned");
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ __align__(8) uint64_t bar[2];  // [0]: zs slot, [1]: momentum slot
-  __shared__ float coef[3];
   // the dynamic region starts after the static variables: the slots begin at
   // its first 128-byte boundary (the launch adds 128 bytes)
   unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
@@ -554,15 +522,17 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     if (tid == 0 && my > 0) load_zs(blockIdx.x);  // zs was written two kernels back (pass X)
     build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
   }
-  if (CONF) kick_coefs(a, coef, tid);  // read after the first barrier of the tile loop
-
   const DevScalars* sc = a.sc;  // written by the finalize three kernels back
   float zshA = 0.f, zshB = 0.f;
   if (AXIS == 2 && !RUNS) {
     zshA = (float)__ldcg(&sc->mean[0]);
     zshB = (float)__ldcg(&sc->mean[1]);
   }
-  float ck = (float)a.hk, cv = (float)a.hk;  // static background; expanding: coef[] after the first barrier
+  float ck = (float)a.hk, cv = (float)a.hk;  // static background
+  if (CONF) {  // expanding: the kick's coefficients, left by the kernel before pass X
+    ck = __ldcg(&sc->co[1]);
+    cv = __ldcg(&sc->co[2]);
+  }
   ModelP mp = a.model;
   if constexpr (MODEL >= 0) mp.model = MODEL;
   KSum ge, ke;
@@ -578,10 +548,6 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     }
     fail = !mbar_wait(&bar[0], ph);
     if (__syncthreads_or(fail)) break;
-    if (CONF && j == 0) {
-      ck = coef[1];
-      cv = coef[2];
-    }
     float vr[Q], vi[Q];
     float hA[AXIS == 2 ? Q : 1], hB[AXIS == 2 ? Q : 1];
 #pragma unroll

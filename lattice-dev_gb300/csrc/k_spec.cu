@@ -333,8 +333,10 @@ __global__ void state_reset_kernel(DevScalars* sc) {
   if (!isfinite(sc->ke_cur)) sc->ke_cur = 0.0;
 }
 
-// sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur
-__global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb) {
+// sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur,
+// and the coefficients of the call's first streamed kick into sc->co
+__global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb, KickW first,
+                           double Nd) {
   // first kernel of a streamed call, launched with programmatic serialization
   // (the wait returns at once when nothing precedes it programmatically)
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
@@ -349,6 +351,7 @@ __global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars
   if (grid_reduce<1>(vals, rb, tot)) {
     sc->ke_cur = tot[0];
     if (bad(tot[0])) sc->err |= 1u;
+    if (first.valid) kick_coefs_of(sc->a, sc->ap, tot[0], first.hd, first.hk, first.hg, Nd, sc->co);
   }
 }
 
@@ -373,7 +376,10 @@ int launch_kmul(const KmulArgs& a, int precision, cudaStream_t s) {
 // block order, then the scalar chain of the kick (hamiltonian_conformal.f90:
 // 86-174): the drift's ysclp += hd KE2/a^3, a1 = a - hg ysclp/6, the kick's
 // ysclp -= a1^3 (GE2/a1^2 + 4 PE) hk, a = a1 - hg ysclp/6; and the lattice
-// means, the shifts of the next kick.
+// means, the shifts of the next kick; and the FP32 coefficients of the next
+// kick of the call (kick_coefs_of), which its three passes load.  The chain
+// runs in one thread between pass Z and the next pass X, so its quotients
+// use one reciprocal per scale factor (a0, a1) and products by 1/N and 1/6.
 __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
   // warp w < 7 sums value w of the seven (pass X: pe, GEx, sum phi_A, sum
   // phi_B; Y: GEy; Z: GEz, sum pi^2) over the blocks, all loads of a lane in
@@ -413,17 +419,21 @@ __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
   w->gsum[1] = tot[4];
   w->gsum[2] = tot[5];
   if (f.conf) {
-    const double a0 = w->a, ke = w->ke_cur;
-    const double ap0 = w->ap + f.hd * (ke / f.Nd) / (a0 * a0 * a0);
-    const double a1 = a0 - f.hg * ap0 / 6.0;
-    const double GE2 = (tot[1] + tot[4] + tot[5]) / (a1 * a1) / f.Nd;
-    const double PE = tot[0] / f.Nd;
+    const double a0 = w->a, ke = w->ke_cur, iN = 1.0 / f.Nd, hg6 = f.hg * (1.0 / 6.0);
+    const double r0 = 1.0 / a0;
+    const double ap0 = w->ap + f.hd * ke * iN * (r0 * r0 * r0);
+    const double a1 = a0 - hg6 * ap0;
+    const double r1 = 1.0 / a1;
+    const double GE2 = (tot[1] + tot[4] + tot[5]) * iN * (r1 * r1);
+    const double PE = tot[0] * iN;
     const double ap1 = ap0 - a1 * a1 * a1 * (GE2 + 4.0 * PE) * f.hk;
+    const double a2 = a1 - hg6 * ap1;
     w->pe = PE;
     if (f.hd != 0.0) w->ke2 = ke;
     w->ap = ap1;
-    w->a = a1 - f.hg * ap1 / 6.0;
+    w->a = a2;
     w->ke_cur = tot[6];
+    if (f.next.valid) kick_coefs_of(a2, ap1, tot[6], f.next.hd, f.next.hk, f.next.hg, f.Nd, w->co);
     if (bad(PE) || bad(GE2) || bad(tot[6])) w->err |= 1u;
   }
   if (bad(tot[2]) || bad(tot[3])) w->err |= 1u;
@@ -437,9 +447,11 @@ int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s) {
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "separable finalize launch");
 }
 
-int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s) {
+int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s, KickW first,
+                   double Nd) {
   if (n % 4) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
-  cudaError_t e = launch_pdl(pi2_kernel, dim3(grid), dim3(256), 0, s, static_cast<const float4*>(pi), n / 4, sc, rb);
+  cudaError_t e = launch_pdl(pi2_kernel, dim3(grid), dim3(256), 0, s, static_cast<const float4*>(pi), n / 4, sc, rb,
+                             first, Nd);
   if (e != cudaSuccess) return cuda_fail(e, "momenta sum launch");
   if (g_launch_counter) ++*g_launch_counter;
   e = cudaGetLastError();
