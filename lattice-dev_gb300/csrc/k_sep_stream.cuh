@@ -7,10 +7,14 @@
 // kick in this form, line A and line B forming one complex line:
 //
 //   pass X: drift of phi (Kahan), z = (phi - shift) - c written as the FP32
-//           array zs (lines A and B interleaved), pi += ck d2x(z)  [PE, GEx, means]
+//           array zs (lines A and B interleaved),
+//           pi += ck d2x(z) - cv V'(z + shift)               [PE, GEx, means]
 //   pass Y: pi += ck d2y(zs)                                 [GEy]
-//   pass Z: pi += ck d2z(zs) - cv V'(zs + shift)             [GEz, sum pi^2]
+//   pass Z: pi += ck d2z(zs)                                 [GEz, sum pi^2]
 //
+// The potential force belongs to the pass that holds the drifted fields in
+// registers (X, whose loads leave issue slots free); evaluated in pass Z it
+// cost that pass 32 registers of z + shift and 9 us of its 78 us at 256^3.
 // with ck = hk a1^2, cv = hk a1^4, a1 = a - hg ysclp / 6 after the drift's
 // ysclp += hd sum(pi^2)/N / a^3 (hamiltonian_conformal.f90:86-174).  The
 // momenta accumulate the kick pass by pass, so no Laplacian array is kept:
@@ -284,8 +288,9 @@ __device__ __forceinline__ void stage_rows_x(const SepArgs& a, float* dst, int64
   }
 }
 
-// Pass X: drift, zs and the x part of the kick.
-template <int N, bool RUNS, bool CONF>
+// Pass X: drift, zs, the potential force and the x part of the kick.
+// MODEL >= 0: the potential fixed at compile time; -1: read from the arguments.
+template <int N, bool RUNS, bool CONF, int MODEL = -1>
 __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     sep_stream_x(const __grid_constant__ SepArgs a) {
   using T = STile<0, N>;
@@ -333,11 +338,14 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
     shBf = (float)__ldcg(&sc->mean[1]);
   }
   const bool drift = a.hd != 0.0;
-  float cd = (float)a.hd, ck = (float)a.hk;
+  float cd = (float)a.hd, ck = (float)a.hk, cv = (float)a.hk;
   if (CONF) {  // the kick's coefficients, left by the kernel before it (read after the wait above)
     cd = __ldcg(&sc->co[0]);
     ck = __ldcg(&sc->co[1]);
+    cv = __ldcg(&sc->co[2]);
   }
+  ModelP mp = a.model;
+  if constexpr (MODEL >= 0) mp.model = MODEL;
   KSum ge, pe, mA, mB;
   // pairs of runs: each run's shift is its phi at site 0 after the previous
   // kick (shift_b), loaded one tile ahead; the block holding a pair's first
@@ -392,7 +400,7 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       if (!RUNS) {
         if (CONF) {
           float ff[2] = {fA, fB};
-          pes[q % 4] += model_v<float, 2>(a.model, ff);
+          pes[q % 4] += model_v<float, 2>(mp, ff);
         }
         mAs[q % 4] += fA;
         mBs[q % 4] += fB;
@@ -400,6 +408,22 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
       vr[q] = (fA - shA) - cA;
       vi[q] = (fB - shB) - cB;
       zs2[pos] = make_float2(vr[q], vi[q]);
+      // the potential force at the drifted, compensated fields (zs + shift)
+      float dA, dB;
+      if constexpr (RUNS) {  // two independent runs: each its own potential
+        float fa[1] = {vr[q] + shA}, fb[1] = {vi[q] + shB}, da[1], db[1];
+        model_dv<float, 1>(mp, fa, da);
+        model_dv<float, 1>(mp, fb, db);
+        dA = da[0];
+        dB = db[0];
+      } else {
+        float ff[2] = {vr[q] + shA, vi[q] + shB}, dv[2];
+        model_dv<float, 2>(mp, ff, dv);
+        dA = dv[0];
+        dB = dv[1];
+      }
+      pA[q] = pA[q] - cv * dA;
+      pB[q] = pB[q] - cv * dB;
     }
     if (!RUNS) {
       pe.add((pes[0] + pes[1]) + (pes[2] + pes[3]));
@@ -424,9 +448,9 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
   block_partials<4>(vals, a.rb.partials + SEP_PART_X);
 }
 
-// Passes Y (AXIS 1: the y part of the kick) and Z (AXIS 2: the z part with
-// the potential force, which completes the kick; its ysclp update follows in
-// launch_sep_finalize).  A tile's zs rows (64 KB at 256 points) and both
+// Passes Y (AXIS 1: the y part of the kick) and Z (AXIS 2: the z part, which
+// completes the kick; its ysclp update follows in launch_sep_finalize; the
+// potential force was added by pass X, whose fields are in registers).  A tile's zs rows (64 KB at 256 points) and both
 // lines' momentum rows arrive by one TMA tensor copy each (zs: a 4D box,
 // the momenta of lines A and B: one 5D box; the last dimension is the pair
 // of runs, 1 for the two fields of a lattice), counted on an mbarrier per
@@ -440,12 +464,10 @@ __global__ void __launch_bounds__(STile<0, N>::THREADS, STile<0, N>::MINB)
 // only the momenta) loads and transforms its first zs tile while Y drains.
 // A bounded mbarrier wait that gives up sets bit 1 of the scalar block's
 // error word (reported as LAT_ERR_TIMEOUT) and the block leaves.
-// MODEL >= 0: the potential fixed at compile time (the model switch folds
-// away in pass Z); -1: read from the arguments.
 // RUNS: pairs of one-field runs, each line with its own shift (the run's phi
-// at site 0 after the previous kick, from pass X) and its own potential;
-// pass Z hands the new site-0 values to the next pass X.
-template <int AXIS, int N, bool RUNS, bool CONF, int MODEL = -1>
+// at site 0 after the previous kick); pass Z hands the new site-0 values
+// (zs + the shift pass X took) to the next pass X.
+template <int AXIS, int N, bool RUNS, bool CONF>
 __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     sep_stream_yz_tma(const __grid_constant__ SepArgs a) {
   using T = STile<AXIS, N>;
@@ -523,18 +545,8 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     build_tables<N>(static_cast<const float2*>(a.twN), (float)a.dk2, tf, ti, fk, tid, T::THREADS);
   }
   const DevScalars* sc = a.sc;  // written by the finalize three kernels back
-  float zshA = 0.f, zshB = 0.f;
-  if (AXIS == 2 && !RUNS) {
-    zshA = (float)__ldcg(&sc->mean[0]);
-    zshB = (float)__ldcg(&sc->mean[1]);
-  }
-  float ck = (float)a.hk, cv = (float)a.hk;  // static background
-  if (CONF) {  // expanding: the kick's coefficients, left by the kernel before pass X
-    ck = __ldcg(&sc->co[1]);
-    cv = __ldcg(&sc->co[2]);
-  }
-  ModelP mp = a.model;
-  if constexpr (MODEL >= 0) mp.model = MODEL;
+  float ck = (float)a.hk;  // static background
+  if (CONF) ck = __ldcg(&sc->co[1]);  // expanding: the kick's coefficient, left by the kernel before pass X
   KSum ge, ke;
   int fail = 0;
   for (int j = 0; j < my; ++j) {
@@ -542,30 +554,22 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     const uint32_t ph = (uint32_t)(j & 1);
     int pr, x0, o;
     coords(tile, pr, x0, o);
-    if (RUNS && AXIS == 2) {  // the shifts pass X took for the two runs of this pair
-      zshA = __ldcg(a.shift_a + 2 * pr);
-      zshB = __ldcg(a.shift_a + 2 * pr + 1);
-    }
     fail = !mbar_wait(&bar[0], ph);
     if (__syncthreads_or(fail)) break;
     float vr[Q], vi[Q];
-    float hA[AXIS == 2 ? Q : 1], hB[AXIS == 2 ? Q : 1];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int pos = t + P * q;
       const float2 z = reinterpret_cast<const float2*>(es)[pos * T::RS + li];
       vr[q] = z.x;
       vi[q] = z.y;
-      if constexpr (AXIS == 2) {
-        hA[q] = vr[q] + zshA;  // phi - c
-        hB[q] = vi[q] + zshB;
-      }
     }
     if constexpr (RUNS && AXIS == 2) {
       if (t == 0 && li == 0 && ((uint32_t)tile * LINES) % (uint32_t)a.pair_lines == 0) {
-        // site 0 of both runs of the pair: the next pass X's shifts
-        a.shift_b[2 * pr] = hA[0];
-        a.shift_b[2 * pr + 1] = hB[0];
+        // site 0 of both runs of the pair (zs + the shift pass X took): the
+        // next pass X's shifts
+        a.shift_b[2 * pr] = vr[0] + __ldcg(a.shift_a + 2 * pr);
+        a.shift_b[2 * pr + 1] = vi[0] + __ldcg(a.shift_a + 2 * pr + 1);
       }
     }
     __syncthreads();  // every thread has its zs: the slot takes the next tile
@@ -589,27 +593,9 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
       const int pos = t + P * q;
       const float* pa = ls + pos * T::RS + li;
       float pA = pa[0], pB = pa[T::ARR];
-      if constexpr (AXIS == 1) {
-        pA = pA + ck * vr[q];
-        pB = pB + ck * vi[q];
-      } else {
-        float dA, dB;
-        if constexpr (RUNS) {  // two independent runs: each its own potential
-          float fa[1] = {hA[q]}, fb[1] = {hB[q]}, da[1], db[1];
-          model_dv<float, 1>(mp, fa, da);
-          model_dv<float, 1>(mp, fb, db);
-          dA = da[0];
-          dB = db[0];
-        } else {
-          float ff[2] = {hA[q], hB[q]}, dv[2];
-          model_dv<float, 2>(mp, ff, dv);
-          dA = dv[0];
-          dB = dv[1];
-        }
-        pA = pA + (ck * vr[q] - cv * dA);
-        pB = pB + (ck * vi[q] - cv * dB);
-        if (CONF) kes[q % 4] += pA * pA + pB * pB;
-      }
+      pA = pA + ck * vr[q];
+      pB = pB + ck * vi[q];
+      if (AXIS == 2 && CONF) kes[q % 4] += pA * pA + pB * pB;
       pi_o[offA + (int64_t)pos * st] = pA;
       pi_o[offB + (int64_t)pos * st] = pB;
     }
@@ -686,14 +672,15 @@ int sep_stream_dispatch(const SepArgs& a, int axis, cudaStream_t s) {
   if constexpr (!RUNS) {
     if (a.conf) {
       switch (axis) {
-        case 0: return stream_launch(sep_stream_x<N, false, true>, STile<0, N>::SMEM, STile<0, N>::THREADS,
-                                     STile<0, N>::MINB, ntiles, a, s, true);
+        case 0:
+          if (a.model.model == LAT_MODEL_PHI4_G2)  // the headline model: the potential folds at compile time
+            return stream_launch(sep_stream_x<N, false, true, LAT_MODEL_PHI4_G2>, STile<0, N>::SMEM,
+                                 STile<0, N>::THREADS, STile<0, N>::MINB, ntiles, a, s, true);
+          return stream_launch(sep_stream_x<N, false, true>, STile<0, N>::SMEM, STile<0, N>::THREADS,
+                               STile<0, N>::MINB, ntiles, a, s, true);
         case 1: return stream_launch(sep_stream_yz_tma<1, N, false, true>, TY::SMEM + 128, TY::THREADS, TY::MINB,
                                      ntiles, a, s, true);
         default:
-          if (a.model.model == LAT_MODEL_PHI4_G2)
-            return stream_launch(sep_stream_yz_tma<2, N, false, true, LAT_MODEL_PHI4_G2>, TZ::SMEM + 128, TZ::THREADS,
-                                 TZ::MINB, ntiles, a, s, true);
           return stream_launch(sep_stream_yz_tma<2, N, false, true>, TZ::SMEM + 128, TZ::THREADS, TZ::MINB, ntiles,
                                a, s, true);
       }
