@@ -633,7 +633,7 @@ def fd_workloads(L, hbm):
     g.autotune(os.environ.get("LAT_TUNE_CACHE"))
     dt = 0.25 / 10
     g.symp(2, dt, 3)
-    K = 20
+    K = 100  # one symp2 call; its leading and trailing half drifts are timed with it
     g.prepare_symp(2, dt, K)
     g.sync()
     g.mark(0)

@@ -5,7 +5,8 @@ lattice energy up to an error of the integrator's order: halving dt over the
 same time divides the energy drift by 2^order (4 for symp2, 16 for symp4).
 The FP32-Kahan streamed passes must keep the energy (Minkowski) and the
 Friedmann constraint (expanding background) within 1e-6 over the headline
-model's first 100 steps.
+model's first 100 steps, and a run split into several calls must follow one
+call of the same steps.
 """
 from __future__ import annotations
 
@@ -14,6 +15,7 @@ import math
 import numpy as np
 import pytest
 
+from conftest import rel_err
 from helpers import L, random_state
 
 pytestmark = pytest.mark.gpu
@@ -72,3 +74,33 @@ def test_fp32_kahan_streamed_conserves_energy_and_friedmann(engine):
     g.close()
     print(f"FP32-Kahan Friedmann residual after 100 steps: {res:.2e}")
     assert abs(res) <= 1e-6
+
+
+def test_streamed_calls_chunked_match_one_call(engine):
+    """The first kick of every call takes its coefficients from the momentum
+    sum that starts the call, the later kicks from the previous kick's
+    finalize: four calls of 3 steps follow one call of 12 steps to FP32
+    rounding (the two sums of pi^2 differ only in their summation order),
+    and a(t) to 1e-12."""
+    n = 128
+    length = 10 * math.pi * n / 256
+    dt = length / n / 20
+    c = L.make_config(n, nfld=2, length=length, laplacian=L.LAP_SPECTRAL, background=L.BG_CONFORMAL,
+                      precision=L.FP32_KAHAN, model=L.MODEL_PHI4_G2, model_params=(1.0, 2.0),
+                      spectral_impl=L.SPEC_IMPL_SEPARABLE)
+    out = []
+    for calls, steps in ((1, 12), (4, 3)):
+        g = engine.Lattice(c)
+        assert g.sep_streamed()
+        f, p = random_state((2, n, n, n), seed=23, mean=1.0, amp=0.05)
+        g.set_state(f, p)
+        g.set_scale_factor(1.0, 0.0)
+        g.calc_metric()
+        for _ in range(calls):
+            g.symp(4, dt, steps)
+        out.append((g.get_state(), g.scale_factor()))
+        g.close()
+    ((f1, p1), (a1, ap1)), ((f4, p4), (a4, ap4)) = out
+    print(f"chunked vs one call: fields {rel_err(f4, f1):.2e} momenta {rel_err(p4, p1):.2e} a {abs(a4 - a1) / a1:.2e}")
+    assert rel_err(f4, f1) <= 1e-6 and rel_err(p4, p1) <= 1e-5
+    assert abs(a4 - a1) <= 1e-12 * a1 and abs(ap4 - ap1) <= 1e-8 * abs(ap1)
