@@ -59,6 +59,18 @@ __device__ __forceinline__ void kick_coefs_of(double a0, double ap, double ke, d
   c[2] = (float)(k1 * a1 * a1);
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor in the stream drains.  It
+// must call pdl_wait() before it reads anything the predecessor writes
+// (wait returns once the predecessor grid has completed and its memory is
+// visible; without a programmatic predecessor it returns at once).  Every
+// kernel of such a chain calls pdl_trigger() only after its own pdl_wait(),
+// so a kernel's successor never starts before the kernel's own predecessor
+// has completed: anything written two kernels back may be read before the
+// wait.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // Reduction scratch: one partial row per block plus an arrival counter.
 struct RedBuf {
   double* partials;       // [max_blocks * 16]

@@ -47,6 +47,11 @@ constexpr int kFdMaxSlots = 4;  // halo'd plane elements one thread stages per p
 
 template <typename R, bool KAHAN, int NF, bool GW, bool SEVEN, int MODE>
 __global__ void __launch_bounds__(512) fd_kernel(FdArgs a) {
+  // launched as a programmatic dependent: every array may have been written
+  // by the previous pass, so nothing is read before the wait; the next pass
+  // (usually the next step's) launches while this one runs
+  pdl_wait();
+  pdl_trigger();
   constexpr int NC = NF + (GW ? 6 : 0);
   constexpr int TX = 32;
   const int TY = blockDim.y;
@@ -321,6 +326,8 @@ __device__ __forceinline__ void fd2_row(const float* row, int tx, float& l, floa
 
 template <bool KAHAN, int NF, bool GW, bool SEVEN, int MODE>
 __global__ void __launch_bounds__(256) fd2_kernel(FdArgs a) {
+  pdl_wait();  // a programmatic dependent, as fd_kernel
+  pdl_trigger();
   using R = float;
   constexpr int NC = NF + (GW ? 6 : 0);
   constexpr int Wd = kFd2Wd;
@@ -634,10 +641,11 @@ int go2(const FdArgs& a, cudaStream_t s, int* nb) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "fd2 smem attribute");
   }
-  k<<<grid, block, smem, s>>>(a);
+  cudaError_t e = launch_pdl(k, grid, block, smem, s, a);
+  if (e != cudaSuccess) return cuda_fail(e, "fd2 kernel launch");
   if (nb) *nb = grid.x * grid.y * grid.z;
   if (g_launch_counter) ++*g_launch_counter;
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "fd2 kernel launch");
 }
 
@@ -659,10 +667,11 @@ int go(const FdArgs& a0, cudaStream_t s, int* nb) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "fd smem attribute");
   }
-  k<<<grid, block, smem, s>>>(a);
+  cudaError_t e = launch_pdl(k, grid, block, smem, s, a);
+  if (e != cudaSuccess) return cuda_fail(e, "fd kernel launch");
   if (nb) *nb = grid.x * grid.y * grid.z;
   if (g_launch_counter) ++*g_launch_counter;
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   return e == cudaSuccess ? LAT_OK : cuda_fail(e, "fd kernel launch");
 }
 

@@ -311,18 +311,6 @@ __device__ __forceinline__ void cp16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Programmatic dependent launch: a kernel launched with programmatic stream
-// serialization may start while its predecessor in the stream drains.  It
-// must call pdl_wait() before it reads anything the predecessor writes
-// (wait returns once the predecessor grid has completed and its memory is
-// visible; without a programmatic predecessor it returns at once).  Every
-// kernel of such a chain calls pdl_trigger() only after its own pdl_wait(),
-// so a kernel's successor never starts before the kernel's own predecessor
-// has completed: anything written two kernels back may be read before the
-// wait.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
-
 // Tile geometry of a pass: 256 threads, LINES = 256/P complex lines per
 // block.  The FFT scratch of one line is padded so that the lines sharing a
 // warp start in different shared-memory banks.
