@@ -254,7 +254,8 @@ __device__ __forceinline__ void d2_line(R (&re)[Split<N>::Q], R (&im)[Split<N>::
     ge.add(gpart * (R)(1.0 / N));
     dft<P, true, R>(ur[g], ui[g]);
   }
-  __syncthreads();
+  // no barrier here: rows kq = t + g P are read and rewritten by thread t
+  // alone; the next barrier orders them before the column reads
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int kq = t + g * P;

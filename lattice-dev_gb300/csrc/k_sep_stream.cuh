@@ -115,7 +115,8 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
     if (GE) ge.add(((gp[0] + gp[1]) + (gp[2] + gp[3])) * (1.0f / N));
     dft<P, true, float>(ur[g], ui[g]);
   }
-  sync();
+  // no barrier here: rows kq = t + g P are read and rewritten by thread t
+  // alone; the next barrier orders them before the column reads
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int kq = t + g * P;
@@ -554,8 +555,9 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
     const uint32_t ph = (uint32_t)(j & 1);
     int pr, x0, o;
     coords(tile, pr, x0, o);
+    // every thread waits on the slot's barrier itself; the barrier that
+    // releases the slot also makes a timeout the whole block's decision
     fail = !mbar_wait(&bar[0], ph);
-    if (__syncthreads_or(fail)) break;
     float vr[Q], vi[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
         a.shift_b[2 * pr + 1] = vi[0] + __ldcg(a.shift_a + 2 * pr + 1);
       }
     }
-    __syncthreads();  // every thread has its zs: the slot takes the next tile
+    if (__syncthreads_or(fail)) break;  // every thread has its zs: the slot takes the next tile
     if (tid == 0 && j + 1 < my) {
       fence_proxy_async();
       load_zs(tile + (int)gridDim.x);
@@ -584,7 +586,6 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
       if (tid == 0) load_pi(tile);
     }
     fail = !mbar_wait(&bar[1], ph);
-    if (__syncthreads_or(fail)) break;
     const int64_t offA = (int64_t)pr * 2 * Nsite + (AXIS == 1 ? (int64_t)o * a.nx * a.ny : (int64_t)o * a.nx) + x0 + li;
     const int64_t offB = Nsite + offA;
     float kes[4] = {0.f, 0.f, 0.f, 0.f};
@@ -600,7 +601,7 @@ __global__ void __launch_bounds__(STile<AXIS, N>::THREADS, STile<AXIS, N>::MINB)
       pi_o[offB + (int64_t)pos * st] = pB;
     }
     if (AXIS == 2 && CONF) ke.add((kes[0] + kes[1]) + (kes[2] + kes[3]));
-    __syncthreads();  // every thread has read its momenta: the slot takes the next tile
+    if (__syncthreads_or(fail)) break;  // every thread has read its momenta: the slot takes the next tile
     if (tid == 0 && j + 1 < my) {
       fence_proxy_async();
       load_pi(tile + (int)gridDim.x);
