@@ -44,8 +44,8 @@ template <> struct Split<64> { static constexpr int P = 8, Q = 8; };
 template <> struct Split<128> { static constexpr int P = 8, Q = 16; };
 template <> struct Split<256> { static constexpr int P = 16, Q = 16; };
 template <> struct Split<512> { static constexpr int P = 16, Q = 32; };
-template <> struct Split<96> { static constexpr int P = 4, Q = 24; };   // Q = 3 x 8 (dft24)
-template <> struct Split<192> { static constexpr int P = 8, Q = 24; };
+template <> struct Split<96> { static constexpr int P = 8, Q = 12; };   // Q = 3 x 4 (dft12); 12 rows over 8 threads
+template <> struct Split<192> { static constexpr int P = 8, Q = 24; };  // Q = 3 x 8 (dft24)
 
 template <typename R> struct Cx;
 template <> struct Cx<float> {
@@ -138,15 +138,15 @@ __device__ __forceinline__ void dft_stage(Rt (&re)[R], Rt (&im)[R]) {
 }
 
 template <int R, bool INV, typename Rt>
-__device__ __forceinline__ void dft24(Rt (&re)[R], Rt (&im)[R]);
+__device__ __forceinline__ void dft3m(Rt (&re)[R], Rt (&im)[R]);
 
 // In-register DFT on separate real and imaginary arrays, natural order in and
 // out: radix 2 for R <= 64 points (R a power of two; W_len^k from the
-// constant table), and R = 24 = 3 x 8.
+// constant table), and R = 12 = 3 x 4 and 24 = 3 x 8.
 template <int R, bool INV, typename Rt>
 __device__ __forceinline__ void dft(Rt (&re)[R], Rt (&im)[R]) {
-  if constexpr (R == 24) {
-    dft24<R, INV, Rt>(re, im);
+  if constexpr (R == 24 || R == 12) {
+    dft3m<R, INV, Rt>(re, im);
   } else {
     static_assert(R >= 2 && R <= 64 && (R & (R - 1)) == 0, "register DFT length must be a power of two <= 64 or 24");
     bitrev_perm<R>(re, im, std::make_integer_sequence<int, R>{});
@@ -154,28 +154,30 @@ __device__ __forceinline__ void dft(Rt (&re)[R], Rt (&im)[R]) {
   }
 }
 
-// 24-point DFT by decimation in time over 3: the three 8-point DFTs of the
-// subsequences x[3 n1 + n2] (Y_n2[k1]), twiddles W_24^{n2 k1}, then 3-point
-// DFTs over n2 give X[k1 + 8 k2].  The 3-point DFT with w = exp(-+2 pi i / 3):
+// 3M-point DFT (M = 4 or 8) by decimation in time over 3: the three M-point
+// DFTs of the subsequences x[3 n1 + n2] (Y_n2[k1]), twiddles
+// W_3M^{n2 k1} = W_24^{(8/M) n2 k1}, then 3-point DFTs over n2 give
+// X[k1 + M k2].  The 3-point DFT with w = exp(-+2 pi i / 3):
 // X0 = a + s, X1,2 = a - s/2 -+ i (sqrt(3)/2) d, s = b + c, d = b - c.
 template <int R, bool INV, typename Rt>
-__device__ __forceinline__ void dft24(Rt (&re)[R], Rt (&im)[R]) {
-  static_assert(R == 24, "dft24 takes 24 points");
-  Rt ar[3][8], ai[3][8];
+__device__ __forceinline__ void dft3m(Rt (&re)[R], Rt (&im)[R]) {
+  static_assert(R == 24 || R == 12, "dft3m takes 12 or 24 points");
+  constexpr int M = R / 3, TS = 8 / M;
+  Rt ar[3][M], ai[3][M];
 #pragma unroll
   for (int n2 = 0; n2 < 3; ++n2) {
 #pragma unroll
-    for (int n1 = 0; n1 < 8; ++n1) {
+    for (int n1 = 0; n1 < M; ++n1) {
       ar[n2][n1] = re[3 * n1 + n2];
       ai[n2][n1] = im[3 * n1 + n2];
     }
-    dft<8, INV, Rt>(ar[n2], ai[n2]);
+    dft<M, INV, Rt>(ar[n2], ai[n2]);
   }
 #pragma unroll
   for (int n2 = 1; n2 < 3; ++n2) {
 #pragma unroll
-    for (int k1 = 1; k1 < 8; ++k1) {
-      const auto w = Cx<Rt>::tw24(n2 * k1);
+    for (int k1 = 1; k1 < M; ++k1) {
+      const auto w = Cx<Rt>::tw24(TS * n2 * k1);
       const Rt xr = ar[n2][k1], xi = ai[n2][k1];
       if (INV) {  // times conj(w)
         ar[n2][k1] = xr * w.x + xi * w.y;
@@ -188,22 +190,22 @@ __device__ __forceinline__ void dft24(Rt (&re)[R], Rt (&im)[R]) {
   }
   const Rt h3 = (Rt)0.8660254037844386;  // sqrt(3)/2
 #pragma unroll
-  for (int k1 = 0; k1 < 8; ++k1) {
+  for (int k1 = 0; k1 < M; ++k1) {
     const Rt sr = ar[1][k1] + ar[2][k1], si = ai[1][k1] + ai[2][k1];
     const Rt dr = (ar[1][k1] - ar[2][k1]) * h3, di = (ai[1][k1] - ai[2][k1]) * h3;
     const Rt tr = ar[0][k1] - (Rt)0.5 * sr, ti = ai[0][k1] - (Rt)0.5 * si;
     re[k1] = ar[0][k1] + sr;
     im[k1] = ai[0][k1] + si;
     if (INV) {  // X1 = t + i m, X2 = t - i m
-      re[k1 + 8] = tr - di;
-      im[k1 + 8] = ti + dr;
-      re[k1 + 16] = tr + di;
-      im[k1 + 16] = ti - dr;
+      re[k1 + M] = tr - di;
+      im[k1 + M] = ti + dr;
+      re[k1 + 2 * M] = tr + di;
+      im[k1 + 2 * M] = ti - dr;
     } else {    // X1 = t - i m, X2 = t + i m
-      re[k1 + 8] = tr + di;
-      im[k1 + 8] = ti - dr;
-      re[k1 + 16] = tr - di;
-      im[k1 + 16] = ti + dr;
+      re[k1 + M] = tr + di;
+      im[k1 + M] = ti - dr;
+      re[k1 + 2 * M] = tr - di;
+      im[k1 + 2 * M] = ti + dr;
     }
   }
 }
@@ -217,6 +219,7 @@ template <int N, typename R, typename C, typename Acc>
 __device__ __forceinline__ void d2_line(R (&re)[Split<N>::Q], R (&im)[Split<N>::Q], int t, C* sl, const C* twN, R dk2,
                                         Acc& ge) {
   constexpr int P = Split<N>::P, Q = Split<N>::Q, G = Q / P, S = P + 1;
+  static_assert(Q % P == 0, "the one-tile passes need Q a multiple of P");
   dft<Q, false, R>(re, im);
 #pragma unroll
   for (int kq = 0; kq < Q; ++kq) {

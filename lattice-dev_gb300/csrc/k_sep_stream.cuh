@@ -75,8 +75,10 @@ template <int K> __device__ __forceinline__ void cp_wait_keep() {
 template <int N, bool WARP, bool GE, typename Acc>
 __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im)[Split<N>::Q], int t, float2* sl,
                                             const float2* tf, const float2* ti, const float* fk, Acc& ge) {
-  constexpr int P = Split<N>::P, Q = Split<N>::Q, G = Q / P, S = P + 1;
-  static_assert(Q % P == 0, "the transform needs Q a multiple of P");
+  // G rows kq = t + g P of the transposed line per thread; when P does not
+  // divide Q (96 = 8 x 12) the last row group covers only kq < Q
+  constexpr int P = Split<N>::P, Q = Split<N>::Q, G = (Q + P - 1) / P, S = P + 1;
+  static_assert(Q >= P, "the transform needs Q >= P");
   auto sync = [] {
     if (WARP) __syncwarp();
     else __syncthreads();
@@ -94,6 +96,7 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int kq = t + g * P;
+    if (Q % P != 0 && kq >= Q) break;  // (uniform per thread: the last group)
 #pragma unroll
     for (int tt = 0; tt < P; ++tt) {
       const float2 z = sl[kq * S + tt];
@@ -120,6 +123,7 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int kq = t + g * P;
+    if (Q % P != 0 && kq >= Q) break;
     const float2* tik = ti + kq;
 #pragma unroll
     for (int mp = 0; mp < P; ++mp) {
