@@ -45,7 +45,7 @@ template <> struct Split<128> { static constexpr int P = 8, Q = 16; };
 template <> struct Split<256> { static constexpr int P = 16, Q = 16; };
 template <> struct Split<512> { static constexpr int P = 16, Q = 32; };
 template <> struct Split<96> { static constexpr int P = 8, Q = 12; };   // Q = 3 x 4 (dft12); 12 rows over 8 threads
-template <> struct Split<192> { static constexpr int P = 8, Q = 24; };  // Q = 3 x 8 (dft24)
+template <> struct Split<192> { static constexpr int P = 16, Q = 12; };  // Q = 3 x 4 (dft12); 12 rows over 16 threads
 
 template <typename R> struct Cx;
 template <> struct Cx<float> {

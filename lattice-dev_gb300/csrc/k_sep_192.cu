@@ -1,5 +1,5 @@
 // k_sep_192.cu -- streamed separable passes for pairs of one-field runs on
-// lines of 192 points (24-point register DFTs).
+// lines of 192 points (16 threads x 12-point register DFTs).
 #include "k_sep_stream.cuh"
 
 namespace lat {

@@ -1,5 +1,5 @@
 // k_sep_96.cu -- streamed separable passes for pairs of one-field runs on
-// lines of 96 points (24-point register DFTs).
+// lines of 96 points (8 threads x 12-point register DFTs).
 #include "k_sep_stream.cuh"
 
 namespace lat {

@@ -76,9 +76,9 @@ template <int N, bool WARP, bool GE, typename Acc>
 __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im)[Split<N>::Q], int t, float2* sl,
                                             const float2* tf, const float2* ti, const float* fk, Acc& ge) {
   // G rows kq = t + g P of the transposed line per thread; when P does not
-  // divide Q (96 = 8 x 12) the last row group covers only kq < Q
+  // divide Q (96 = 8 x 12, 192 = 16 x 12) the last row group covers only
+  // kq < Q and the threads past it sit out the middle phase
   constexpr int P = Split<N>::P, Q = Split<N>::Q, G = (Q + P - 1) / P, S = P + 1;
-  static_assert(Q >= P, "the transform needs Q >= P");
   auto sync = [] {
     if (WARP) __syncwarp();
     else __syncthreads();
