@@ -67,7 +67,7 @@ template <int K> __device__ __forceinline__ void cp_wait_keep() {
 // Spectral second derivative of one complex line, as d2_line (k_sep.cuh) but
 // with per-block tables instead of per-point index arithmetic:
 // tf[kq * P + t] = W_N^{t kq} and ti[mp * Q + kq] = W_N^{mp kq} (the same
-// table when P == Q), fk[k] = (f dk)^2 for wavenumber index k.  Every table
+// table when P == Q), fk[k] = -(f dk)^2 / N for wavenumber index k.  Every table
 // read is the thread's base plus a compile-time offset.  WARP: the P threads
 // of every line sit in one warp, so the transposes need only warp barriers.
 // GE: add the axis' Parseval sum (f dk)^2 |Z_k|^2 / N to `ge` (only an
@@ -85,8 +85,9 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
   };
   dft<Q, false, float>(re, im);
   const float2* tft = tf + t;
+  sl[t] = make_float2(re[0], im[0]);  // kq = 0: W_N^0 = 1 on every thread
 #pragma unroll
-  for (int kq = 0; kq < Q; ++kq) {
+  for (int kq = 1; kq < Q; ++kq) {
     const float2 w = tft[kq * P];
     const float xr = re[kq], xi = im[kq];
     sl[kq * S + t] = make_float2(xr * w.x - xi * w.y, xr * w.y + xi * w.x);
@@ -104,18 +105,17 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
       ui[g][tt] = z.y;
     }
     dft<P, false, float>(ur[g], ui[g]);
-    const float* fkk = fk + kq;  // k = kq + Q kp
+    const float* fkk = fk + kq;  // k = kq + Q kp; fk holds -(f dk)^2 / N
     float gp[4] = {0.f, 0.f, 0.f, 0.f};  // four independent partial sums
 #pragma unroll
     for (int kp = 0; kp < P; ++kp) {
-      const float f2 = fkk[Q * kp];
+      const float h = fkk[Q * kp];
       const float zr = ur[g][kp], zi = ui[g][kp];
-      if (GE) gp[kp % 4] += f2 * (zr * zr + zi * zi);
-      const float h = -f2 * (1.0f / N);
+      if (GE) gp[kp % 4] += h * (zr * zr + zi * zi);
       ur[g][kp] = zr * h;
       ui[g][kp] = zi * h;
     }
-    if (GE) ge.add(((gp[0] + gp[1]) + (gp[2] + gp[3])) * (1.0f / N));
+    if (GE) ge.add(-((gp[0] + gp[1]) + (gp[2] + gp[3])));
     dft<P, true, float>(ur[g], ui[g]);
   }
   // no barrier here: rows kq = t + g P are read and rewritten by thread t
@@ -125,8 +125,9 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
     const int kq = t + g * P;
     if (Q % P != 0 && kq >= Q) break;
     const float2* tik = ti + kq;
+    sl[kq * S] = make_float2(ur[g][0], ui[g][0]);  // mp = 0: W_N^0 = 1 on every thread
 #pragma unroll
-    for (int mp = 0; mp < P; ++mp) {
+    for (int mp = 1; mp < P; ++mp) {
       const float2 w = tik[mp * Q];
       const float xr = ur[g][mp], xi = ui[g][mp];
       sl[kq * S + mp] = make_float2(xr * w.x + xi * w.y, xi * w.x - xr * w.y);  // times conj(W_N^{mp kq})
@@ -142,7 +143,8 @@ __device__ __forceinline__ void d2_line_tab(float (&re)[Split<N>::Q], float (&im
   dft<Q, true, float>(re, im);
 }
 
-// Build the tables of d2_line_tab from W_N^j (global) in shared memory.
+// Build the tables of d2_line_tab from W_N^j (global) in shared memory:
+// tf, ti as above, fk[k] = -(f dk)^2 / N.
 template <int N>
 __device__ __forceinline__ void build_tables(const float2* twN, float dk2, float2* tf, float2* ti, float* fk, int tid,
                                              int nthreads) {
@@ -151,9 +153,9 @@ __device__ __forceinline__ void build_tables(const float2* twN, float dk2, float
     tf[j] = twN[((j % P) * (j / P)) % N];
     if (P != Q) ti[j] = twN[((j / Q) * (j % Q)) % N];
   }
-  for (int k = tid; k < N; k += nthreads) {
+  for (int k = tid; k < N; k += nthreads) {  // the multiplier of the second derivative, with the 1/N
     const int f = k <= N / 2 ? k : k - N;
-    fk[k] = (float)(f * f) * dk2;
+    fk[k] = -((float)(f * f) * dk2) * (1.0f / N);
   }
 }
 
