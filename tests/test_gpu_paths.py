@@ -213,7 +213,7 @@ def test_streamed_passes_match_classic(engine, shape, conf, monkeypatch):
 
 def test_ensemble_streamed_passes(engine, monkeypatch):
     """Ensembles whose size classes admit the streamed separable passes (two
-    runs of a class as one complex line, 24-point register DFTs for 96 and 192)
+    runs of a class as one complex line, 12-point register DFTs for 96 and 192)
     against the FP64 ensemble (cuFFT) and the FP32 cuFFT ensemble from the
     same initial states."""
     sizes = [64, 96, 64, 96, 128, 192, 128, 192]
