@@ -139,18 +139,97 @@ __device__ __forceinline__ void dft_stage(Rt (&re)[R], Rt (&im)[R]) {
 
 template <int R, bool INV, typename Rt>
 __device__ __forceinline__ void dft3m(Rt (&re)[R], Rt (&im)[R]);
+template <bool INV, typename Rt>
+__device__ __forceinline__ void dft16r4(Rt (&re)[16], Rt (&im)[16]);
 
 // In-register DFT on separate real and imaginary arrays, natural order in and
-// out: radix 2 for R <= 64 points (R a power of two; W_len^k from the
-// constant table), and R = 12 = 3 x 4 and 24 = 3 x 8.
+// out: radix 4 for R = 16, radix 2 for the other powers of two up to 64
+// points (W_len^k from the constant table), and R = 12 = 3 x 4 and
+// 24 = 3 x 8.
 template <int R, bool INV, typename Rt>
 __device__ __forceinline__ void dft(Rt (&re)[R], Rt (&im)[R]) {
   if constexpr (R == 24 || R == 12) {
     dft3m<R, INV, Rt>(re, im);
+  } else if constexpr (R == 16) {
+    dft16r4<INV, Rt>(re, im);
   } else {
     static_assert(R >= 2 && R <= 64 && (R & (R - 1)) == 0, "register DFT length must be a power of two <= 64 or 24");
     bitrev_perm<R>(re, im, std::make_integer_sequence<int, R>{});
     dft_stage<R, INV, Rt, 2>(re, im);
+  }
+}
+
+// 4-point DFT of (a, b, c, d) in place: y0 = (a + c) + (b + d),
+// y2 = (a + c) - (b + d), y1,3 = (a - c) -+ i (b - d) forward (+- inverse).
+template <bool INV, typename Rt>
+__device__ __forceinline__ void dft4_at(Rt (&re)[16], Rt (&im)[16], int i0, int i1, int i2, int i3) {
+  const Rt sr = re[i0] + re[i2], si = im[i0] + im[i2];
+  const Rt dr = re[i0] - re[i2], di = im[i0] - im[i2];
+  const Rt tr = re[i1] + re[i3], ti = im[i1] + im[i3];
+  const Rt ur = re[i1] - re[i3], ui = im[i1] - im[i3];
+  re[i0] = sr + tr;
+  im[i0] = si + ti;
+  re[i2] = sr - tr;
+  im[i2] = si - ti;
+  if (INV) {  // y1 = d + i u, y3 = d - i u
+    re[i1] = dr - ui;
+    im[i1] = di + ur;
+    re[i3] = dr + ui;
+    im[i3] = di - ur;
+  } else {    // y1 = d - i u, y3 = d + i u
+    re[i1] = dr + ui;
+    im[i1] = di - ur;
+    re[i3] = dr - ui;
+    im[i3] = di + ur;
+  }
+}
+
+// 16-point DFT by decimation in time over 4 (radix 4): the four 4-point DFTs
+// A_n2[k1] of x[4 n1 + n2], twiddles W_16^{n2 k1} (W_64^{4 n2 k1} from the
+// constant table; W_16^4 = -i is a swap), then 4-point DFTs over n2 give
+// X[k1 + 4 k2].  160 real additions and multiplications against 168 for
+// four radix-2 stages.
+template <bool INV, typename Rt>
+__device__ __forceinline__ void dft16r4(Rt (&re)[16], Rt (&im)[16]) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4_at<INV, Rt>(re, im, n2, n2 + 4, n2 + 8, n2 + 12);  // A_n2[k1] at 4 k1 + n2
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2) {
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1) {
+      const int j = 4 * k1 + n2, m = n2 * k1;
+      const Rt xr = re[j], xi = im[j];
+      if (m == 4) {  // W_16^4 = -i (forward), +i (inverse)
+        if (INV) { re[j] = -xi; im[j] = xr; }
+        else { re[j] = xi; im[j] = -xr; }
+      } else {
+        const auto w = Cx<Rt>::tw(4 * m);
+        if (INV) {  // times conj(w)
+          re[j] = xr * w.x + xi * w.y;
+          im[j] = xi * w.x - xr * w.y;
+        } else {
+          re[j] = xr * w.x - xi * w.y;
+          im[j] = xr * w.y + xi * w.x;
+        }
+      }
+    }
+  }
+  // X[k1 + 4 k2] = sum over n2 of B_n2[k1] W_4^{n2 k2}: 4-point DFTs across
+  // n2 of the values at 4 k1 + n2, written back in natural order
+  Rt orr[16], oi[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    dft4_at<INV, Rt>(re, im, 4 * k1, 4 * k1 + 1, 4 * k1 + 2, 4 * k1 + 3);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      orr[k1 + 4 * k2] = re[4 * k1 + k2];
+      oi[k1 + 4 * k2] = im[4 * k1 + k2];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    re[k] = orr[k];
+    im[k] = oi[k];
   }
 }
 
