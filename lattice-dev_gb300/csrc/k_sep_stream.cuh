@@ -12,12 +12,12 @@
 //   pass Y: pi += ck d2y(zs)                                 [GEy]
 //   pass Z: pi += ck d2z(zs)                                 [GEz, sum pi^2]
 //
-// The potential force belongs to the pass that holds the drifted fields in
-// registers (X, whose loads leave issue slots free); evaluated in pass Z it
-// cost that pass 32 registers of z + shift and 9 us of its 78 us at 256^3.
 // with ck = hk a1^2, cv = hk a1^4, a1 = a - hg ysclp / 6 after the drift's
 // ysclp += hd sum(pi^2)/N / a^3 (hamiltonian_conformal.f90:86-174).  The
-// momenta accumulate the kick pass by pass, so no Laplacian array is kept:
+// potential force belongs to the pass that holds the drifted fields in
+// registers (X, whose loads leave issue slots free); evaluated in pass Z it
+// cost that pass 32 registers of z + shift and 9 us of its 78 us at 256^3.
+// The momenta accumulate the kick pass by pass, so no Laplacian array is kept:
 // per line and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
 // needs ck before it has seen all momenta, so sum pi^2 comes from the pass Z
 // of the previous kick (or one reduction before the first pass X of a call).
@@ -45,9 +45,13 @@
 // The two-field chain X, Y, Z, finalize (pairs of runs: Y, Z) is launched
 // with programmatic dependent launch: each pass starts while its predecessor drains and waits
 // (griddepcontrol.wait) only before reading what the predecessor writes.
-// Pass X stages the phi and c of its first tile early (last written by the
-// previous pass X), pass Z its first zs tile and that tile's transform (zs
-// comes from pass X; pass Y writes only the momenta).  The passes load the
+// Pass X stages its whole first tile early (phi and c were last written by
+// the previous pass X, the momenta by the previous pass Z, both complete
+// before its predecessor let it start), pass Z its first zs tile and that
+// tile's transform (zs comes from pass X; pass Y writes only the momenta).
+// Y and Z wait on each slot's mbarrier per thread and take four block
+// barriers per tile (two release the slots, two order the transposes).
+// The passes load the
 // kick's FP32 coefficients (cd, ck, cv: kick_coefs_of) from the scalar block,
 // where the single-block kernel before pass X (the previous kick's finalize,
 // or the momentum sum that starts a call) left them: at GB300's FP64 rate the
