@@ -676,10 +676,12 @@ int exec_sep(lat_s* h, const std::vector<Op>& ops) {
     return LAT_ERR_UNSUPPORTED;
   }
   double pending = lead;
-  if (h->sep_stream && conf && !grp.empty()) {  // sum pi^2 and the coefficients of the first kick
+  if (h->sep_stream && !grp.empty()) {
+    // the fields' means (the first kick's shifts) and, expanding, sum pi^2 and
+    // the coefficients of the first kick
     Timed t(h, LAT_K_OTHER);
     RET(launch_pi2_sum(h->fldp, (int64_t)h->nf * h->N, h->sc, red(h), 2 * h->nsm, h->stream,
-                       KickW{grp[0].hk, grp[0].hg, lead, 1}, (double)h->N));
+                       KickW{grp[0].hk, grp[0].hg, lead, conf ? 1 : 0}, (double)h->N, h->fld[h->cur], h->N));
   }
   for (size_t gi = 0; gi < grp.size(); ++gi) {
     const Grp& g = grp[gi];

@@ -184,9 +184,12 @@ struct KickW {
   double hk, hg, hd;
   int valid;
 };
-// sum pi^2 into sc->ke_cur; with first.valid also the first kick's coefficients into sc->co
+// sum pi^2 into sc->ke_cur; with phi (two FP32 fields of nsite sites) the
+// fields' means into sc->mean; with first.valid the first kick's coefficients
+// into sc->co
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s,
-                   KickW first = KickW{0.0, 0.0, 0.0, 0}, double Nd = 1.0);
+                   KickW first = KickW{0.0, 0.0, 0.0, 0}, double Nd = 1.0, const void* phi = nullptr,
+                   int64_t nsite = 0);
 // Partials of the streamed passes of one kick in the reduction buffer: pass X
 // [grid][pe, GEx, sum phi_A, sum phi_B] at SEP_PART_X, pass Y [grid][GEy],
 // pass Z [grid][GEz, sum pi^2]; completed after pass Z by launch_sep_finalize.

@@ -20,7 +20,8 @@
 // The momenta accumulate the kick pass by pass, so no Laplacian array is kept:
 // per line and kick the passes move 28 + 12 + 12 bytes per site.  Pass X
 // needs ck before it has seen all momenta, so sum pi^2 comes from the pass Z
-// of the previous kick (or one reduction before the first pass X of a call).
+// of the previous kick (or one reduction before the first pass X of a call,
+// which also takes the fields' means: the first kick's shifts).
 // The passes only write per-block partial sums; one single-block kernel after
 // pass Z (launch_sep_finalize) completes them in block order and advances
 // the scale factor, so no pass ends on a grid-wide arrival counter and the

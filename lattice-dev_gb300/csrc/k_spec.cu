@@ -333,24 +333,46 @@ __global__ void state_reset_kernel(DevScalars* sc) {
   if (!isfinite(sc->ke_cur)) sc->ke_cur = 0.0;
 }
 
-// sum pi^2 over all fields (FP32 momenta, n a multiple of 4) into sc->ke_cur,
-// and the coefficients of the call's first streamed kick into sc->co
-__global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, DevScalars* sc, RedBuf rb, KickW first,
-                           double Nd) {
-  // first kernel of a streamed call, launched with programmatic serialization
-  // (the wait returns at once when nothing precedes it programmatically)
+// The first kernel of a streamed call: sum pi^2 over all fields (FP32
+// momenta, n a multiple of 4) into sc->ke_cur; with phi, the lattice means of
+// the two fields' phi_hi (q4 float4 per field) into sc->mean, the shifts of
+// the call's first kick (after an upload, an initial condition or steps on
+// another path the last kick's means are stale, and a shift far from the mean
+// leaves the FP32 passes a large constant to transform: a one-time error of
+// 1e-6 in the momenta of the 128^3 preheating lattice); and the coefficients
+// of the call's first kick into sc->co.
+__global__ void pi2_kernel(const float4* __restrict__ pi, int64_t n4, const float4* __restrict__ phi, int64_t q4,
+                           DevScalars* sc, RedBuf rb, KickW first, double Nd) {
+  // launched with programmatic serialization (the wait returns at once when
+  // nothing precedes it programmatically)
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
-  KSum s;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+  KSum s, ma, mb;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = i0; i < n4; i += step) {
     const float4 v = __ldcs(pi + i);
     s.add((v.x * v.x + v.y * v.y) + (v.z * v.z + v.w * v.w));
   }
-  const FF vals[1] = {s.red()};
-  double tot[1];
-  if (grid_reduce<1>(vals, rb, tot)) {
+  if (phi) {
+    for (int64_t i = i0; i < q4; i += step) {
+      const float4 v = __ldcg(phi + i);
+      ma.add((v.x + v.y) + (v.z + v.w));
+    }
+    for (int64_t i = i0; i < q4; i += step) {
+      const float4 v = __ldcg(phi + q4 + i);
+      mb.add((v.x + v.y) + (v.z + v.w));
+    }
+  }
+  const FF vals[3] = {s.red(), ma.red(), mb.red()};
+  double tot[3];
+  if (grid_reduce<3>(vals, rb, tot)) {
     sc->ke_cur = tot[0];
     if (bad(tot[0])) sc->err |= 1u;
+    if (phi) {
+      sc->mean[0] = tot[1] / Nd;
+      sc->mean[1] = tot[2] / Nd;
+      if (bad(tot[1]) || bad(tot[2])) sc->err |= 1u;
+    }
     if (first.valid) kick_coefs_of(sc->a, sc->ap, tot[0], first.hd, first.hk, first.hg, Nd, sc->co);
   }
 }
@@ -448,10 +470,10 @@ int launch_sep_finalize(const SepFinArgs& f, cudaStream_t s) {
 }
 
 int launch_pi2_sum(const void* pi, int64_t n, DevScalars* sc, RedBuf rb, int grid, cudaStream_t s, KickW first,
-                   double Nd) {
-  if (n % 4) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
-  cudaError_t e = launch_pdl(pi2_kernel, dim3(grid), dim3(256), 0, s, static_cast<const float4*>(pi), n / 4, sc, rb,
-                             first, Nd);
+                   double Nd, const void* phi, int64_t nsite) {
+  if (n % 4 || (phi && nsite % 4)) return set_error(LAT_ERR_STATE, "momenta sum: length not a multiple of 4");
+  cudaError_t e = launch_pdl(pi2_kernel, dim3(grid), dim3(256), 0, s, static_cast<const float4*>(pi), n / 4,
+                             static_cast<const float4*>(phi), phi ? nsite / 4 : int64_t{0}, sc, rb, first, Nd);
   if (e != cudaSuccess) return cuda_fail(e, "momenta sum launch");
   if (g_launch_counter) ++*g_launch_counter;
   e = cudaGetLastError();
