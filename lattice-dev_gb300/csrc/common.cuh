@@ -32,7 +32,6 @@ struct DevScalars {
   double red[16];  // raw sums of the last stand-alone reduction (energies)
   double gsum[3];  // -sum phi d2_axis(phi) of the separable passes X, Y, Z
   double mean[4];  // lattice means of the fields (spectral shift of the separable passes)
-  double zsh[2];   // shift the zs array of the last streamed kick was taken with (k_sep_stream.cuh)
   double ke_cur;   // sum pi^2 of the current momenta, kept by the streamed passes
   float co[4];     // FP32 cd, ck, cv of the next streamed kick (kick_coefs_of), from the kernel before it
   unsigned int err;  // bit 0: NaN/Inf met in a reduction; bit 1: a bounded device wait gave up

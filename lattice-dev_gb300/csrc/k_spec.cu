@@ -328,8 +328,6 @@ __global__ void state_reset_kernel(DevScalars* sc) {
   sc->err = 0u;
   for (int i = 0; i < 4; ++i)
     if (!isfinite(sc->mean[i])) sc->mean[i] = 0.0;
-  for (int i = 0; i < 2; ++i)
-    if (!isfinite(sc->zsh[i])) sc->zsh[i] = 0.0;
   if (!isfinite(sc->ke_cur)) sc->ke_cur = 0.0;
 }
 
@@ -433,8 +431,6 @@ __global__ void __launch_bounds__(256) sep_finalize_kernel(SepFinArgs f) {
   if (threadIdx.x != 0) return;
   // tot: pe, GEx, sum phi_A, sum phi_B, GEy, GEz, sum pi^2
   DevScalars* w = f.sc;
-  w->zsh[0] = w->mean[0];  // the shift this kick's zs was taken with
-  w->zsh[1] = w->mean[1];
   w->mean[0] = tot[2] / f.Nd;
   w->mean[1] = tot[3] / f.Nd;
   w->gsum[0] = tot[1];
